@@ -1,0 +1,24 @@
+"""gputucker_gb300 -- GB300-native sparse Tucker ALS (the GPUTucker factor-update path).
+
+The compute path is the native library libgputucker_gb300.so (hand-written
+sm_103a CUDA kernels behind a C ABI, include/gputucker_gb300.h); this package
+is a thin host binding over it.
+"""
+
+from ._native import GTKError, LIB_PATH  # noqa: F401
+from .tucker import (  # noqa: F401
+    BlockedTensor,
+    Coo,
+    coo_from_arrays,
+    create_tensor_blocks,
+    generate,
+    generate_planted,
+    parse_buffer,
+    parse_from_file,
+    tucker_decomposition,
+)
+
+__all__ = [
+    "GTKError", "LIB_PATH", "BlockedTensor", "Coo", "coo_from_arrays", "create_tensor_blocks", "generate",
+    "generate_planted", "parse_buffer", "parse_from_file", "tucker_decomposition",
+]

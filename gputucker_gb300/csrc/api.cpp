@@ -1,0 +1,603 @@
+// api.cpp -- the C ABI (include/gputucker_gb300.h): handle lifecycle, readback,
+// initialisation and the sweep driver.  Returns status codes; never exits.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace gtk {
+
+int parse_buffer(const char *buf, size_t len, int N, int dtype, uint32_t seed, gtk_coo *out);
+int parse_file(const char *path, int N, int dtype, uint32_t seed, gtk_coo *out);
+
+namespace {
+thread_local std::string g_err;
+constexpr int kPartialDoubles = 2048;
+
+uint64_t memory_cap() {
+  const char *s = getenv("GTK_DEVICE_MEMORY_CAP");
+  if (!s || !*s) return 0;
+  return strtoull(s, nullptr, 10);
+}
+}  // namespace
+
+void set_error(const std::string &msg) { g_err = msg; }
+int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+int cuda_fail(cudaError_t e, const char *what) {
+  g_err = std::string(what) + ": " + cudaGetErrorString(e);
+  cudaGetLastError();  // clear a non-sticky error so the context stays usable
+  return e == cudaErrorMemoryAllocation ? GTK_ERR_OOM : GTK_ERR_CUDA;
+}
+
+// Device allocation owned by the handle; honours GTK_DEVICE_MEMORY_CAP (bytes).
+int dalloc(DevTensor &t, void **p, size_t bytes) {
+  if (bytes < 16) bytes = 16;
+  bytes = (bytes + 255) / 256 * 256;
+  uint64_t cap = memory_cap();
+  if (cap && t.bytes + bytes > cap)
+    return fail(GTK_ERR_OOM, "device memory cap (GTK_DEVICE_MEMORY_CAP) exceeded");
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(GTK_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  t.allocs.push_back(*p);
+  t.bytes += bytes;
+  return 0;
+}
+
+static void release(DevTensor &t) {
+  if (t.dev >= 0) cudaSetDevice(t.dev);
+  if (t.stream) cudaStreamSynchronize(t.stream);
+  for (void *p : t.allocs) cudaFree(p);
+  t.allocs.clear();
+  if (t.tev0) cudaEventDestroy(t.tev0);
+  if (t.tev1) cudaEventDestroy(t.tev1);
+  if (t.stream) cudaStreamDestroy(t.stream);
+  t.stream = nullptr;
+}
+
+// slab layout [rows][J] <-> device [rows][ldf]
+static int put_factor(DevTensor &t, int n, const void *slabs) {
+  GTK_CUDA(cudaMemcpy2DAsync(t.fac[n], (size_t)t.ldf * t.vsize, slabs, (size_t)t.J * t.vsize, (size_t)t.J * t.vsize,
+                             t.rows[n], cudaMemcpyHostToDevice, t.stream));
+  GTK_CUDA(cudaStreamSynchronize(t.stream));
+  return 0;
+}
+
+static int get_factor(const DevTensor &t, int n, void *slabs) {
+  GTK_CUDA(cudaMemcpy2DAsync(slabs, (size_t)t.J * t.vsize, t.fac[n], (size_t)t.ldf * t.vsize, (size_t)t.J * t.vsize,
+                             t.rows[n], cudaMemcpyDeviceToHost, t.stream));
+  GTK_CUDA(cudaStreamSynchronize(t.stream));
+  return 0;
+}
+
+static int put_core(DevTensor &t, const void *core) {
+  GTK_CUDA(cudaMemcpyAsync(t.core, core, t.core_n * t.vsize, cudaMemcpyHostToDevice, t.stream));
+  if (int rc = upload_core_perms(t, core)) return rc;
+  t.have_core = true;
+  return 0;
+}
+
+static int check_status(DevTensor &t) {
+  int st = 0;
+  GTK_CUDA(cudaMemcpyAsync(&st, t.status, 4, cudaMemcpyDeviceToHost, t.stream));
+  GTK_CUDA(cudaStreamSynchronize(t.stream));
+  if (st) {
+    GTK_CUDA(cudaMemsetAsync(t.status, 0, 4, t.stream));
+    return fail(GTK_ERR_NUMERIC, "a row solve met a non-positive pivot");
+  }
+  return 0;
+}
+
+}  // namespace gtk
+
+using namespace gtk;
+
+#define GTK_GUARD_BEGIN try {
+#define GTK_GUARD_END                                         \
+  }                                                           \
+  catch (std::bad_alloc &) {                                  \
+    return fail(GTK_ERR_OOM, "host allocation failed");       \
+  }                                                           \
+  catch (std::exception & e) {                                \
+    return fail(GTK_ERR_ARG, e.what());                       \
+  }
+
+static int set_dev(const gtk_tensor *t) {
+  GTK_CUDA(cudaSetDevice(t->dev));
+  return 0;
+}
+
+extern "C" {
+
+const char *gtk_last_error(void) { return g_err.c_str(); }
+int gtk_version(void) { return GTK_VERSION; }
+
+int gtk_parse_buffer(const char *buf, size_t len, int order, int dtype, uint32_t rand_seed, gtk_coo **out) {
+  if (!out || (!buf && len)) return fail(GTK_ERR_ARG, "null argument");
+  GTK_GUARD_BEGIN
+  gtk_coo *c = new gtk_coo();
+  int rc = parse_buffer(buf, len, order, dtype, rand_seed, c);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_parse_file(const char *path, int order, int dtype, uint32_t rand_seed, gtk_coo **out) {
+  if (!path || !out) return fail(GTK_ERR_ARG, "null argument");
+  GTK_GUARD_BEGIN
+  gtk_coo *c = new gtk_coo();
+  int rc = parse_file(path, order, dtype, rand_seed, c);
+  if (rc) {
+    delete c;
+    return rc;
+  }
+  *out = c;
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_coo_from_arrays(int order, uint64_t nnz, const uint32_t *const *idx, const void *values, int dtype,
+                        const uint32_t *dims, gtk_coo **out) {
+  if (!out || (nnz && (!idx || !values))) return fail(GTK_ERR_ARG, "null argument");
+  if (order < 1 || order > GTK_MAX_ORDER) return fail(GTK_ERR_ARG, "order must be 1..8");
+  if (dtype != GTK_F32 && dtype != GTK_F64) return fail(GTK_ERR_ARG, "bad dtype");
+  GTK_GUARD_BEGIN
+  gtk_coo *c = new gtk_coo();
+  c->N = order;
+  c->dtype = dtype;
+  c->nnz = nnz;
+  for (int n = 0; n < order; ++n) {
+    if (nnz && !idx[n]) {
+      delete c;
+      return fail(GTK_ERR_ARG, "null index array");
+    }
+    c->idx[n].assign(idx[n], idx[n] + nnz);
+    uint32_t mx = 0;
+    for (uint64_t k = 0; k < nnz; ++k) mx = std::max(mx, idx[n][k]);
+    if (dims) {
+      if (nnz && mx >= dims[n]) {
+        delete c;
+        return fail(GTK_ERR_ARG, "coordinate out of bounds");
+      }
+      c->dims[n] = dims[n];
+    } else {
+      c->dims[n] = nnz ? mx + 1 : 0;
+    }
+  }
+  if (dtype == GTK_F32)
+    c->vf.assign((const float *)values, (const float *)values + nnz);
+  else
+    c->vd.assign((const double *)values, (const double *)values + nnz);
+  *out = c;
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_coo_info(const gtk_coo *c, int *order, int *dtype, uint64_t *nnz, uint32_t *dims, uint64_t *draws) {
+  if (!c) return fail(GTK_ERR_ARG, "null coo");
+  if (order) *order = c->N;
+  if (dtype) *dtype = c->dtype;
+  if (nnz) *nnz = c->nnz;
+  if (dims)
+    for (int n = 0; n < c->N; ++n) dims[n] = c->dims[n];
+  if (draws) *draws = c->draws;
+  return 0;
+}
+
+int gtk_coo_export(const gtk_coo *c, uint32_t *const *idx, void *values) {
+  if (!c) return fail(GTK_ERR_ARG, "null coo");
+  if (idx)
+    for (int n = 0; n < c->N; ++n)
+      if (idx[n]) memcpy(idx[n], c->idx[n].data(), c->nnz * 4);
+  if (values) memcpy(values, c->values(), c->nnz * (c->dtype == GTK_F32 ? 4 : 8));
+  return 0;
+}
+
+int gtk_coo_pin(gtk_coo *c) {
+  if (!c) return fail(GTK_ERR_ARG, "null coo");
+  if (c->pinned || c->nnz == 0) return 0;
+  for (int n = 0; n < c->N; ++n)
+    GTK_CUDA(cudaHostRegister(c->idx[n].data(), c->nnz * 4, cudaHostRegisterDefault));
+  GTK_CUDA(cudaHostRegister(const_cast<void *>(c->values()), c->nnz * (c->dtype == GTK_F32 ? 4 : 8),
+                            cudaHostRegisterDefault));
+  c->pinned = true;
+  return 0;
+}
+
+void gtk_coo_free(gtk_coo *c) {
+  if (!c) return;
+  if (c->pinned) {
+    for (int n = 0; n < c->N; ++n) cudaHostUnregister(c->idx[n].data());
+    cudaHostUnregister(const_cast<void *>(c->values()));
+  }
+  delete c;
+}
+
+int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int device, gtk_tensor **out) {
+  if (!coo || !P || !out) return fail(GTK_ERR_ARG, "null argument");
+  if (rank < 1 || rank > GTK_MAX_RANK) return fail(GTK_ERR_ARG, "rank must be 1..64");
+  const int N = coo->N;
+  if (coo->nnz >= 0xFFFFFFFFull) return fail(GTK_ERR_UNSUPPORTED, "more than 2^32-2 nonzeros");
+  uint64_t nblk = 1;
+  uint32_t bd[GTK_MAX_ORDER];
+  for (int n = 0; n < N; ++n) {
+    if (P[n] == 0) return fail(GTK_ERR_ARG, "partition parameter must be >= 1");
+    if (coo->dims[n] == 0) return fail(GTK_ERR_ARG, "empty tensor dimension");
+    // tensor.tpp:199-213 / optimizer.tpp:360-376
+    bd[n] = (uint32_t)(((uint64_t)coo->dims[n] + P[n] - 1) / P[n]);
+    uint32_t check = (uint32_t)(((uint64_t)coo->dims[n] + bd[n] - 1) / bd[n]);
+    if (check != P[n]) return fail(GTK_ERR_PARTITION, "Block dimension is larger than the tensor dimension.");
+    nblk *= P[n];
+    if (nblk > 0xFFFFFFFFull) return fail(GTK_ERR_UNSUPPORTED, "more than 2^32 blocks");
+  }
+  uint64_t core_n = 1;
+  for (int n = 0; n < N; ++n) {
+    core_n *= (uint64_t)rank;
+    if (core_n > (1ull << 28)) return fail(GTK_ERR_UNSUPPORTED, "core tensor larger than 2^28 entries");
+  }
+  GTK_GUARD_BEGIN
+  gtk_tensor *t = new gtk_tensor();
+  t->dev = device;
+  t->dtype = coo->dtype;
+  t->vsize = coo->dtype == GTK_F32 ? 4 : 8;
+  t->N = N;
+  t->J = rank;
+  const int w = (int)(16 / t->vsize);
+  t->ldf = (rank + w - 1) / w * w;
+  t->E = (rank + 1) * (rank + 2) / 2 - 1;
+  t->nnz = coo->nnz;
+  t->nblk = nblk;
+  t->core_n = core_n;
+  uint64_t max_rows = 0;
+  for (int n = 0; n < N; ++n) {
+    t->dims[n] = coo->dims[n];
+    t->P[n] = P[n];
+    t->bd[n] = bd[n];
+    t->rows[n] = (uint64_t)P[n] * bd[n];
+    max_rows = std::max(max_rows, t->rows[n]);
+  }
+  auto bail = [&](int rc) {
+    release(*t);
+    delete t;
+    return rc;
+  };
+  if (int rc = ck(cudaSetDevice(device), "cudaSetDevice")) return bail(rc);
+  int sms = 0;
+  if (int rc = ck(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device), "device attribute"))
+    return bail(rc);
+  t->num_sms = sms;
+  if (int rc = ck(cudaStreamCreateWithFlags(&t->stream, cudaStreamNonBlocking), "cudaStreamCreate")) return bail(rc);
+  const uint64_t nnz = t->nnz;
+  const size_t vs = t->vsize;
+  int rc = 0;
+  auto A = [&](void **p, size_t b) {
+    if (!rc) rc = dalloc(*t, p, b);
+  };
+  A((void **)&t->blk_ptr, (nblk + 1) * 8);
+  A(&t->blk_val, nnz * vs);
+  for (int n = 0; n < N; ++n) {
+    A((void **)&t->blk_idx[n], nnz * 4);
+    A((void **)&t->count[n], nblk * (uint64_t)(bd[n] + 1) * 8);
+    A((void **)&t->where[n], nnz * 4);
+    A((void **)&t->vperm[n], nnz * 4);
+    A(&t->vval[n], nnz * vs);
+    for (int k = 0; k < N; ++k) A((void **)&t->vidx[n][k], nnz * 4);
+    A(&t->fac[n], t->rows[n] * t->ldf * vs);
+    A(&t->corep[n], (core_n / rank) * t->ldf * vs);
+  }
+  A(&t->core, core_n * vs);
+  A((void **)&t->gram, max_rows * (uint64_t)t->E * 8);
+  A((void **)&t->partial, kPartialDoubles * 8);
+  A((void **)&t->status, 16);
+  if (rc) return bail(rc);
+  for (int n = 0; n < N; ++n) {
+    if ((rc = ck(cudaMemsetAsync(t->fac[n], 0, t->rows[n] * t->ldf * vs, t->stream), "memset"))) return bail(rc);
+    if ((rc = ck(cudaMemsetAsync(t->corep[n], 0, (core_n / rank) * t->ldf * vs, t->stream), "memset"))) return bail(rc);
+  }
+  if ((rc = ck(cudaMemsetAsync(t->status, 0, 16, t->stream), "memset"))) return bail(rc);
+  if ((rc = build_partition(*t, *coo))) return bail(rc);
+  *out = t;
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_tensor_info_get(const gtk_tensor *t, gtk_tensor_info *info) {
+  if (!t || !info) return fail(GTK_ERR_ARG, "null argument");
+  memset(info, 0, sizeof(*info));
+  info->order = t->N;
+  info->rank = t->J;
+  info->dtype = t->dtype;
+  info->device = t->dev;
+  info->nnz = t->nnz;
+  info->block_count = t->nblk;
+  for (int n = 0; n < t->N; ++n) {
+    info->dims[n] = t->dims[n];
+    info->partition_dims[n] = t->P[n];
+    info->block_dims[n] = t->bd[n];
+  }
+  info->norm = t->norm;
+  info->device_bytes = t->bytes;
+  return 0;
+}
+
+int gtk_block_info(const gtk_tensor *t, uint64_t b, uint32_t *coord, uint64_t *nnz) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (b >= t->nblk) return fail(GTK_ERR_ARG, "block id out of range");
+  if (coord) {
+    uint64_t r = b;
+    for (int n = t->N - 1; n >= 0; --n) {
+      coord[n] = (uint32_t)(r % t->P[n]);
+      r /= t->P[n];
+    }
+  }
+  if (nnz) *nnz = t->h_blk_ptr[b + 1] - t->h_blk_ptr[b];
+  return 0;
+}
+
+int gtk_block_data(const gtk_tensor *t, uint64_t b, uint32_t *const *idx, void *values) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (b >= t->nblk) return fail(GTK_ERR_ARG, "block id out of range");
+  if (int rc = set_dev(t)) return rc;
+  const uint64_t s = t->h_blk_ptr[b], n = t->h_blk_ptr[b + 1] - s;
+  if (idx)
+    for (int k = 0; k < t->N; ++k)
+      if (idx[k] && n) GTK_CUDA(cudaMemcpyAsync(idx[k], t->blk_idx[k] + s, n * 4, cudaMemcpyDeviceToHost, t->stream));
+  if (values && n)
+    GTK_CUDA(cudaMemcpyAsync(values, (const char *)t->blk_val + s * t->vsize, n * t->vsize, cudaMemcpyDeviceToHost,
+                             t->stream));
+  GTK_CUDA(cudaStreamSynchronize(t->stream));
+  return 0;
+}
+
+int gtk_block_segments(const gtk_tensor *t, uint64_t b, int mode, uint64_t *count_nnz, uint32_t *where_nnz) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (b >= t->nblk || mode < 0 || mode >= t->N) return fail(GTK_ERR_ARG, "block or mode out of range");
+  if (int rc = set_dev(t)) return rc;
+  const uint64_t s = t->h_blk_ptr[b], n = t->h_blk_ptr[b + 1] - s;
+  const uint64_t rows = (uint64_t)t->bd[mode] + 1;
+  if (count_nnz)
+    GTK_CUDA(cudaMemcpyAsync(count_nnz, t->count[mode] + b * rows, rows * 8, cudaMemcpyDeviceToHost, t->stream));
+  if (where_nnz && n)
+    GTK_CUDA(cudaMemcpyAsync(where_nnz, t->where[mode] + s, n * 4, cudaMemcpyDeviceToHost, t->stream));
+  GTK_CUDA(cudaStreamSynchronize(t->stream));
+  return 0;
+}
+
+void gtk_destroy(gtk_tensor *t) {
+  if (!t) return;
+  release(*t);
+  delete t;
+}
+
+int gtk_init_random(gtk_tensor *t, uint32_t seed, uint64_t skip) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (int rc = set_dev(t)) return rc;
+  GTK_GUARD_BEGIN
+  GlibcRand g(seed);
+  for (uint64_t k = 0; k < skip; ++k) g.next();
+  const int J = t->J;
+  // tucker.cuh:84-97: mode, slab, real rows of the slab, column
+  for (int n = 0; n < t->N; ++n) {
+    std::vector<unsigned char> slab(t->rows[n] * J * t->vsize, 0);
+    for (uint32_t p = 0; p < t->P[n]; ++p) {
+      uint32_t rows = t->bd[n];
+      if (p + 1 == t->P[n]) rows = t->dims[n] - p * t->bd[n];
+      for (uint32_t r = 0; r < rows; ++r)
+        for (int c = 0; c < J; ++c) {
+          const double v = g.frand01<double>();
+          const uint64_t off = ((uint64_t)p * t->bd[n] + r) * J + c;
+          if (t->dtype == GTK_F32)
+            ((float *)slab.data())[off] = (float)v;
+          else
+            ((double *)slab.data())[off] = v;
+        }
+    }
+    if (int rc = put_factor(*t, n, slab.data())) return rc;
+  }
+  // tucker.cuh:117-134: core in linear order
+  std::vector<unsigned char> core(t->core_n * t->vsize);
+  for (uint64_t i = 0; i < t->core_n; ++i) {
+    const double v = g.frand01<double>();
+    if (t->dtype == GTK_F32)
+      ((float *)core.data())[i] = (float)v;
+    else
+      ((double *)core.data())[i] = v;
+  }
+  if (int rc = put_core(*t, core.data())) return rc;
+  t->have_factors = true;
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_set_factor(gtk_tensor *t, int mode, const void *slabs) {
+  if (!t || !slabs) return fail(GTK_ERR_ARG, "null argument");
+  if (mode < 0 || mode >= t->N) return fail(GTK_ERR_ARG, "mode out of range");
+  if (int rc = set_dev(t)) return rc;
+  if (int rc = put_factor(*t, mode, slabs)) return rc;
+  t->have_factors = true;
+  return 0;
+}
+
+int gtk_get_factor(const gtk_tensor *t, int mode, void *slabs) {
+  if (!t || !slabs) return fail(GTK_ERR_ARG, "null argument");
+  if (mode < 0 || mode >= t->N) return fail(GTK_ERR_ARG, "mode out of range");
+  if (int rc = set_dev(t)) return rc;
+  return get_factor(*t, mode, slabs);
+}
+
+int gtk_set_core(gtk_tensor *t, const void *core) {
+  if (!t || !core) return fail(GTK_ERR_ARG, "null argument");
+  if (int rc = set_dev(t)) return rc;
+  GTK_GUARD_BEGIN
+  return put_core(*t, core);
+  GTK_GUARD_END
+}
+
+int gtk_get_core(const gtk_tensor *t, void *core) {
+  if (!t || !core) return fail(GTK_ERR_ARG, "null argument");
+  if (int rc = set_dev(t)) return rc;
+  GTK_CUDA(cudaMemcpyAsync(core, t->core, t->core_n * t->vsize, cudaMemcpyDeviceToHost, t->stream));
+  GTK_CUDA(cudaStreamSynchronize(t->stream));
+  return 0;
+}
+
+int gtk_set_precision(gtk_tensor *t, int precision) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (precision != GTK_PREC_PLAIN) return fail(GTK_ERR_UNSUPPORTED, "only GTK_PREC_PLAIN is built");
+  t->precision = precision;
+  return 0;
+}
+
+static int ready(gtk_tensor *t) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (!t->have_factors || !t->have_core) return fail(GTK_ERR_STATE, "factors and core are not initialised");
+  return set_dev(t);
+}
+
+int gtk_update_mode(gtk_tensor *t, int mode) {
+  if (int rc = ready(t)) return rc;
+  if (mode < 0 || mode >= t->N) return fail(GTK_ERR_ARG, "mode out of range");
+  GTK_GUARD_BEGIN
+  return run_update_mode(*t, mode);
+  GTK_GUARD_END
+}
+
+int gtk_update_factor_matrices(gtk_tensor *t) {
+  if (int rc = ready(t)) return rc;
+  GTK_GUARD_BEGIN
+  for (int n = 0; n < t->N; ++n)
+    if (int rc = run_update_mode(*t, n)) return rc;
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_reconstruction(gtk_tensor *t, double *fit) {
+  if (int rc = ready(t)) return rc;
+  if (!fit) return fail(GTK_ERR_ARG, "null fit");
+  GTK_GUARD_BEGIN
+  if (int rc = run_fit(*t, fit)) return rc;
+  return check_status(*t);
+  GTK_GUARD_END
+}
+
+int gtk_tucker_decomposition(gtk_tensor *t, int max_iters, double tol, double *fits, int *iters) {
+  if (int rc = ready(t)) return rc;
+  if (max_iters < 1) return fail(GTK_ERR_ARG, "max_iters must be >= 1");
+  GTK_GUARD_BEGIN
+  // tucker.cuh:166-187
+  int it = 0;
+  double p_fit = -1, fit = -1;
+  int numeric = 0;
+  while (true) {
+    for (int n = 0; n < t->N; ++n)
+      if (int rc = run_update_mode(*t, n)) return rc;
+    if (int rc = run_fit(*t, &fit)) return rc;
+    if (check_status(*t)) numeric = GTK_ERR_NUMERIC;
+    if (fits) fits[it] = fit;
+    ++it;
+    if (it >= max_iters || (p_fit != -1 && std::fabs(p_fit - fit) <= tol)) break;
+    p_fit = fit;
+  }
+  if (iters) *iters = it;
+  if (numeric) return fail(GTK_ERR_NUMERIC, "a row solve met a non-positive pivot");
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_compute_delta(gtk_tensor *t, int mode, void *delta) {
+  if (int rc = ready(t)) return rc;
+  if (mode < 0 || mode >= t->N || !delta) return fail(GTK_ERR_ARG, "bad mode or null output");
+  GTK_GUARD_BEGIN
+  const size_t bytes = t->nnz * (size_t)t->J * t->vsize;
+  if (!bytes) return 0;
+  void *d = nullptr;
+  GTK_CUDA(cudaMalloc(&d, bytes));
+  int rc = run_delta(*t, mode, d);
+  if (!rc) rc = ck(cudaMemcpyAsync(delta, d, bytes, cudaMemcpyDeviceToHost, t->stream), "delta readback");
+  if (!rc) rc = ck(cudaStreamSynchronize(t->stream), "sync");
+  cudaFree(d);
+  return rc;
+  GTK_GUARD_END
+}
+
+int gtk_profile_enable(gtk_tensor *t, int on) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  t->prof = on != 0;
+  return 0;
+}
+
+int gtk_profile_read(gtk_tensor *t, int kind, double *ms, uint64_t *launches) {
+  if (!t || kind < 0 || kind > 3) return fail(GTK_ERR_ARG, "bad argument");
+  if (int rc = set_dev(t)) return rc;
+  if (int rc = prof_resolve(*t)) return rc;
+  double m = 0;
+  uint64_t c = 0;
+  if (kind == 3) {
+    for (int k = 0; k < 3; ++k) {
+      m += t->prof_ms[k];
+      c += t->prof_n[k];
+    }
+  } else {
+    m = t->prof_ms[kind];
+    c = t->prof_n[kind];
+  }
+  if (ms) *ms = m;
+  if (launches) *launches = c;
+  return 0;
+}
+
+int gtk_profile_reset(gtk_tensor *t) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (int rc = prof_resolve(*t)) return rc;
+  for (int k = 0; k < 4; ++k) {
+    t->prof_ms[k] = 0;
+    t->prof_n[k] = 0;
+  }
+  return 0;
+}
+
+int gtk_timer_begin(gtk_tensor *t) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (int rc = set_dev(t)) return rc;
+  if (!t->tev0) GTK_CUDA(cudaEventCreate(&t->tev0));
+  if (!t->tev1) GTK_CUDA(cudaEventCreate(&t->tev1));
+  GTK_CUDA(cudaEventRecord(t->tev0, t->stream));
+  return 0;
+}
+
+int gtk_timer_end(gtk_tensor *t, double *ms) {
+  if (!t || !t->tev0) return fail(GTK_ERR_STATE, "timer not started");
+  if (int rc = set_dev(t)) return rc;
+  GTK_CUDA(cudaEventRecord(t->tev1, t->stream));
+  GTK_CUDA(cudaEventSynchronize(t->tev1));
+  float m = 0;
+  GTK_CUDA(cudaEventElapsedTime(&m, t->tev0, t->tev1));
+  if (ms) *ms = m;
+  return 0;
+}
+
+int gtk_synchronize(gtk_tensor *t) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (int rc = set_dev(t)) return rc;
+  GTK_CUDA(cudaStreamSynchronize(t->stream));
+  return 0;
+}
+
+}  // extern "C"

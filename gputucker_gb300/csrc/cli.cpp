@@ -1,0 +1,206 @@
+// cli.cpp -- the gputucker_gb300 command line, a drop-in for GPUTucker's main.cu.
+//
+// Options of the reference (cmdline_opts.cpp:27-32): -i/--input (required, a
+// regular file), -o/--order (required), -r/--rank (default 10), -g/--gpus
+// (default 1; this build runs one GPU).  Added: -p/--partition P_1,..,P_N
+// (the reference derives P_n from free GPU memory), --iters (default 3 =
+// kMaxIteration, constants.hpp:17), --tol (default 1e-4 = kLambda, the
+// reference's stopping threshold, tucker.cuh:183), --seed (glibc srand seed,
+// default 1 = the reference's unseeded rand()), --dtype f32|f64 (main.cu:25
+// uses double), --device, --write-factors PREFIX (factor n in the slab layout,
+// one text row per factor row).
+
+#include <sys/stat.h>
+
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gputucker_gb300.h"
+
+static void usage() {
+  printf(
+      "Program Options:\n"
+      "  -h [ --help ]          Display help menu.\n"
+      "  -i [ --input ] arg     Input tensor path\n"
+      "  -o [ --order ] arg     Order\n"
+      "  -r [ --rank ] arg (=10)  Rank\n"
+      "  -g [ --gpus ] arg (=1)   The number of GPUs (this build: 1)\n"
+      "  -p [ --partition ] P1,..,PN (=1,..,1)  Partition parameters\n"
+      "  --iters arg (=3)       Maximum ALS sweeps\n"
+      "  --tol arg (=1e-4)      Stop when |fit - previous fit| <= tol\n"
+      "  --seed arg (=1)        glibc srand() seed of the initialisation\n"
+      "  --dtype f32|f64 (=f64) Value type\n"
+      "  --device arg (=0)      CUDA device\n"
+      "  --write-factors PREFIX Write PREFIX<n>.txt per factor\n");
+}
+
+static double now() {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+#define CHECK(x)                                                             \
+  do {                                                                       \
+    int rc_ = (x);                                                           \
+    if (rc_) {                                                               \
+      fprintf(stderr, "[ERROR] %s failed (%d): %s\n", #x, rc_, gtk_last_error()); \
+      return 1;                                                              \
+    }                                                                        \
+  } while (0)
+
+int main(int argc, char **argv) {
+  std::string input, prefix, parts;
+  int order = -1, rank = 10, gpus = 1, iters = 3, dtype = GTK_F64, device = 0;
+  double tol = 1e-4;
+  unsigned seed = 1;
+  for (int i = 1; i < argc; ++i) {
+    std::string a = argv[i];
+    auto val = [&](const char *name) -> const char * {
+      if (i + 1 >= argc) {
+        fprintf(stderr, "[ERROR] Parsing error : option '%s' requires an argument\n", name);
+        exit(2);
+      }
+      return argv[++i];
+    };
+    if (a == "-h" || a == "--help") {
+      usage();
+      return 0;
+    } else if (a == "-i" || a == "--input") {
+      input = val("input");
+    } else if (a == "-o" || a == "--order") {
+      order = atoi(val("order"));
+    } else if (a == "-r" || a == "--rank") {
+      rank = atoi(val("rank"));
+    } else if (a == "-g" || a == "--gpus") {
+      gpus = atoi(val("gpus"));
+    } else if (a == "-p" || a == "--partition") {
+      parts = val("partition");
+    } else if (a == "--iters") {
+      iters = atoi(val("iters"));
+    } else if (a == "--tol") {
+      tol = atof(val("tol"));
+    } else if (a == "--seed") {
+      seed = (unsigned)strtoul(val("seed"), nullptr, 10);
+    } else if (a == "--dtype") {
+      std::string d = val("dtype");
+      if (d == "f32") dtype = GTK_F32;
+      else if (d == "f64") dtype = GTK_F64;
+      else {
+        fprintf(stderr, "[ERROR] --dtype must be f32 or f64\n");
+        return 2;
+      }
+    } else if (a == "--device") {
+      device = atoi(val("device"));
+    } else if (a == "--write-factors") {
+      prefix = val("write-factors");
+    } else {
+      fprintf(stderr, "[ERROR] Parsing error : unrecognised option '%s'\n", a.c_str());
+      usage();
+      return 2;
+    }
+  }
+  if (input.empty()) {
+    printf("[ERROR] Input file must be specified!!!\n");
+    usage();
+    return 2;
+  }
+  struct stat st;
+  if (stat(input.c_str(), &st) != 0 || !S_ISREG(st.st_mode)) {
+    printf("[ERROR] Input file provided does not exist [%s]\n", input.c_str());
+    return 2;
+  }
+  if (order < 1) {
+    printf("[ERROR] Tensor order must be specified!!!\n");
+    usage();
+    return 2;
+  }
+  if (gpus != 1) {
+    printf("[ERROR] this build runs on one GPU (-g 1); got -g %d\n", gpus);
+    return 2;
+  }
+  std::vector<uint32_t> P(order, 1);
+  if (!parts.empty()) {
+    size_t pos = 0;
+    for (int n = 0; n < order; ++n) {
+      size_t e = parts.find(',', pos);
+      std::string tok = parts.substr(pos, e == std::string::npos ? std::string::npos : e - pos);
+      if (tok.empty()) {
+        printf("[ERROR] -p needs %d comma-separated values\n", order);
+        return 2;
+      }
+      P[n] = (uint32_t)strtoul(tok.c_str(), nullptr, 10);
+      if (e == std::string::npos) {
+        if (n != order - 1) {
+          printf("[ERROR] -p needs %d comma-separated values\n", order);
+          return 2;
+        }
+        break;
+      }
+      pos = e + 1;
+    }
+  }
+  printf("%s\n", input.c_str());
+  printf("Values are %s type.\n", dtype == GTK_F64 ? "double" : "float");
+  double t0 = now();
+  gtk_coo *coo = nullptr;
+  CHECK(gtk_parse_file(input.c_str(), order, dtype, seed, &coo));
+  uint64_t nnz = 0, draws = 0;
+  std::vector<uint32_t> dims(order);
+  CHECK(gtk_coo_info(coo, nullptr, nullptr, &nnz, dims.data(), &draws));
+  printf("Parse time : %lf\n", now() - t0);
+  for (int n = 0; n < order; ++n) printf("Max. dim[%d] = %u\n", n, dims[n]);
+  printf("# nnzs: %llu\n", (unsigned long long)nnz);
+  t0 = now();
+  gtk_tensor *t = nullptr;
+  CHECK(gtk_create_blocks(coo, P.data(), rank, device, &t));
+  gtk_coo_free(coo);
+  gtk_tensor_info info;
+  CHECK(gtk_tensor_info_get(t, &info));
+  printf("Blocking time : %lf\n", now() - t0);
+  for (int n = 0; n < order; ++n) printf("Partition dim[%d] = %u\tBlock dim[%d] = %u\n", n, P[n], n, info.block_dims[n]);
+  printf("# blocks: %llu\n", (unsigned long long)info.block_count);
+  CHECK(gtk_init_random(t, seed, draws));
+  double p_fit = -1, fit = -1;
+  int it = 0;
+  double avg = now();
+  while (true) {
+    double itertime = now(), step = itertime;
+    CHECK(gtk_update_factor_matrices(t));
+    CHECK(gtk_synchronize(t));
+    printf("Factor Time : %lf\n", now() - step);
+    step = now();
+    CHECK(gtk_reconstruction(t, &fit));
+    printf("Recon Time : %lf\n\n", now() - step);
+    ++it;
+    printf("iter %d\t Fit: %.10g\n", it, fit);
+    printf("iter%d :      Fit : %lf\tElapsed Time : %lf\n\n", it, fit, now() - itertime);
+    if (it >= iters || (p_fit != -1 && (p_fit - fit > 0 ? p_fit - fit : fit - p_fit) <= tol)) break;
+    p_fit = fit;
+  }
+  printf("Average sweep time : %lf\n", (now() - avg) / it);
+  if (!prefix.empty()) {
+    for (int n = 0; n < order; ++n) {
+      const size_t rows = (size_t)P[n] * info.block_dims[n];
+      std::vector<double> fd(rows * rank);
+      std::vector<float> ff(rows * rank);
+      CHECK(gtk_get_factor(t, n, dtype == GTK_F64 ? (void *)fd.data() : (void *)ff.data()));
+      std::string path = prefix + std::to_string(n) + ".txt";
+      FILE *f = fopen(path.c_str(), "w");
+      if (!f) {
+        fprintf(stderr, "[ERROR] cannot write %s\n", path.c_str());
+        return 1;
+      }
+      for (size_t r = 0; r < dims[n]; ++r) {
+        for (int c = 0; c < rank; ++c)
+          fprintf(f, c + 1 < rank ? "%.17g\t" : "%.17g\n", dtype == GTK_F64 ? fd[r * rank + c] : (double)ff[r * rank + c]);
+      }
+      fclose(f);
+    }
+  }
+  gtk_destroy(t);
+  printf("DONE\n");
+  return 0;
+}

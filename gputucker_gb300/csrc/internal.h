@@ -1,0 +1,154 @@
+// internal.h -- shared declarations of the gputucker_gb300 library (not installed).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "gputucker_gb300.h"
+
+namespace gtk {
+
+constexpr int kMaxOrder = GTK_MAX_ORDER;
+constexpr int kMaxRank = GTK_MAX_RANK;
+// constants.hpp:18 declares kLambda as a double initialised from the float
+// literal 0.0001f, so its value is float(1e-4) widened to double.
+constexpr double kLambda = (double)0.0001f;
+
+void set_error(const std::string &msg);
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *what);
+
+inline int ck(cudaError_t e, const char *what) { return e == cudaSuccess ? 0 : cuda_fail(e, what); }
+
+#define GTK_CUDA(call)                                      \
+  do {                                                      \
+    cudaError_t e_ = (call);                                \
+    if (e_ != cudaSuccess) return ::gtk::cuda_fail(e_, #call); \
+  } while (0)
+
+// glibc rand(): TYPE_3 additive feedback generator.  r[i] = r[i-31] + r[i-3]
+// (mod 2^32) after a Lehmer (16807 mod 2^31-1, Schrage) seeding of 31 words and
+// 310 discarded outputs; rand() returns r[i] >> 1.  srand(0) behaves as srand(1).
+struct GlibcRand {
+  uint32_t ring[31];
+  uint64_t i = 0;
+  explicit GlibcRand(uint32_t seed) { reseed(seed); }
+  void reseed(uint32_t seed) {
+    int32_t r[34];
+    r[0] = (int32_t)(seed == 0 ? 1u : seed);
+    for (int k = 1; k < 31; ++k) {
+      long long w = r[k - 1];
+      long long hi = w / 127773, lo = w % 127773;
+      w = 16807 * lo - 2836 * hi;
+      if (w < 0) w += 2147483647;
+      r[k] = (int32_t)w;
+    }
+    for (int k = 31; k < 34; ++k) r[k] = r[k - 31];
+    for (int k = 3; k < 34; ++k) ring[k % 31] = (uint32_t)r[k];
+    i = 34;
+    for (int k = 34; k < 344; ++k) step();
+  }
+  inline uint32_t step() {
+    uint32_t v = ring[i % 31] + ring[(i - 3) % 31];
+    ring[i % 31] = v;
+    ++i;
+    return v;
+  }
+  inline int next() { return (int)(step() >> 1); }
+  // frand<T>(0, 1) of the reference (helper.hpp:99)
+  template <class T> inline T frand01() { return (T(1) - T(0)) * (static_cast<T>(next()) / 2147483647) + T(0); }
+};
+
+}  // namespace gtk
+
+// Host-side parsed tensor: one block of global 0-based coordinates.
+struct gtk_coo {
+  int N = 0;
+  int dtype = GTK_F32;
+  uint64_t nnz = 0;
+  uint32_t dims[GTK_MAX_ORDER] = {};
+  std::vector<uint32_t> idx[GTK_MAX_ORDER];
+  std::vector<float> vf;
+  std::vector<double> vd;
+  uint64_t draws = 0;  // rand() draws consumed by lines without a value
+  bool pinned = false;
+  const void *values() const { return dtype == GTK_F32 ? (const void *)vf.data() : (const void *)vd.data(); }
+};
+
+namespace gtk {
+
+// Device buffers of one resident tensor.  Layout in HBM:
+//   blocked arrays (block-major, the reference's Block order):
+//     blk_ptr[nblk+1] u64, blk_idx[n][nnz] u32 local coords, blk_val[nnz] V,
+//     count[n][nblk*(bd_n+1)] u64, where[n][nnz] u32
+//   mode-n views (stable sort by global row i_n of the block-major order, so a
+//   row's nonzeros appear in (block_id, position) order, the order in which
+//   ComputingBC visits them): vidx[n][k][nnz] u32 global coords, vval[n][nnz] V
+//   factor n: rows_n = P_n*bd_n rows of ldf values (ldf = J rounded to 16 bytes)
+//   core: J^N linear; corep[n]: the core with mode n moved to the front,
+//   rows of J values padded to ldf, i.e. [J^(N-1)][ldf]
+//   gram: rows_max x E doubles, E = (J+1)(J+2)/2 - 1 (upper triangle of the
+//   Gram matrix then the right-hand side, see sweep.cu)
+struct DevTensor {
+  int dev = 0;
+  cudaStream_t stream = nullptr;
+  int dtype = GTK_F32;
+  size_t vsize = 4;
+  int N = 0, J = 0, ldf = 0, E = 0;
+  uint64_t nnz = 0, nblk = 1;
+  uint32_t dims[kMaxOrder] = {}, P[kMaxOrder] = {}, bd[kMaxOrder] = {};
+  uint64_t rows[kMaxOrder] = {};
+  uint64_t core_n = 1;
+  double norm = 0;
+  int precision = GTK_PREC_PLAIN;
+  bool have_factors = false, have_core = false;
+
+  std::vector<uint64_t> h_blk_ptr;  // host copy of blk_ptr
+  uint64_t *blk_ptr = nullptr;
+  uint32_t *blk_idx[kMaxOrder] = {};
+  void *blk_val = nullptr;
+  uint64_t *count[kMaxOrder] = {};
+  uint32_t *where[kMaxOrder] = {};
+  uint32_t *vidx[kMaxOrder][kMaxOrder] = {};
+  void *vval[kMaxOrder] = {};
+  uint32_t *vperm[kMaxOrder] = {};  // view position -> block-major position
+  void *fac[kMaxOrder] = {};
+  void *core = nullptr;
+  void *corep[kMaxOrder] = {};
+  double *gram = nullptr;
+  double *partial = nullptr;  // fit partial sums
+  int *status = nullptr;      // device status words (numeric flags)
+  int num_sms = 0;
+
+  // profiling
+  bool prof = false;
+  double prof_ms[4] = {};
+  uint64_t prof_n[4] = {};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
+
+  std::vector<void *> allocs;
+  uint64_t bytes = 0;
+};
+
+// device memory helpers (api.cpp)
+int dalloc(DevTensor &t, void **p, size_t bytes);
+
+// partition.cu
+int build_partition(DevTensor &t, const gtk_coo &coo);
+
+// sweep.cu
+int upload_core_perms(DevTensor &t, const void *core_host);
+int run_update_mode(DevTensor &t, int mode);
+int run_fit(DevTensor &t, double *fit);
+int run_delta(DevTensor &t, int mode, void *d_delta_blockmajor);
+// per-kernel CUDA-event timing on the handle's stream (kind 0 delta+gram, 1 solve, 2 fit)
+int prof_begin(DevTensor &t, cudaEvent_t *a);
+int prof_end(DevTensor &t, int kind, cudaEvent_t a);
+int prof_resolve(DevTensor &t);
+
+}  // namespace gtk
+
+struct gtk_tensor : gtk::DevTensor {};

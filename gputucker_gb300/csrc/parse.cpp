@@ -1,0 +1,235 @@
+// parse.cpp -- the reference's tensor text format, parsed with all host threads.
+//
+// Semantics of _ReadData (tensor_manager.tpp:46-191):
+//   * one nonzero per '\n'; bytes after the last '\n' are ignored (the reference
+//     counts newlines, :88-94);
+//   * tokens are maximal runs of characters other than ' ' and '\t' (strtok_r
+//     with " \t", :134); the first N tokens are indices read with strtoull and
+//     narrowed to uint32 (:135), stored minus one (:143); an index that is 0
+//     after narrowing is an error (:166-169);
+//   * the next token is the value, std::stod narrowed to value_t (:150-151); a
+//     line without one gets frand<value_t>(0,1) (:152-155) -- drawn here in file
+//     order (the reference draws in OpenMP thread order, which equals file order
+//     with one thread);
+//   * dims[n] = the largest index seen (:164-176).
+// Where the reference is undefined this parser reports GTK_ERR_PARSE instead: a
+// line with fewer than N index tokens (the reference reads uninitialised
+// memory; this includes empty lines, which the reference merges with the next
+// line) and a value token strtod cannot read (std::stod throws).
+
+#include <algorithm>
+#include <cerrno>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "internal.h"
+
+namespace gtk {
+namespace {
+
+inline bool is_delim(char c) { return c == ' ' || c == '\t'; }
+
+// strtoull(token, NULL, 10) narrowed to uint32; fast path for plain digit runs
+inline uint32_t parse_index(const char *s, const char *e) {
+  size_t n = (size_t)(e - s);
+  if (n > 0 && n <= 19) {
+    uint64_t v = 0;
+    bool ok = true;
+    for (const char *p = s; p < e; ++p) {
+      unsigned d = (unsigned)(*p - '0');
+      if (d > 9) {
+        ok = false;
+        break;
+      }
+      v = v * 10 + d;
+    }
+    if (ok) return (uint32_t)v;
+  }
+  std::string tok(s, e);
+  return (uint32_t)strtoull(tok.c_str(), nullptr, 10);
+}
+
+struct Chunk {
+  size_t begin = 0, end = 0;  // byte range, whole lines
+  uint64_t lines = 0, first_line = 0;
+  uint32_t maxd[kMaxOrder] = {};
+  uint64_t err_line = UINT64_MAX;
+  int err_code = 0;
+  std::string err_msg;
+};
+
+}  // namespace
+
+int parse_buffer(const char *buf, size_t len, int N, int dtype, uint32_t seed, gtk_coo *out) {
+  if (N < 1 || N > kMaxOrder) return fail(GTK_ERR_ARG, "order must be 1..8");
+  if (dtype != GTK_F32 && dtype != GTK_F64) return fail(GTK_ERR_ARG, "dtype must be GTK_F32 or GTK_F64");
+  // ignore bytes after the last newline
+  size_t eff = 0;
+  for (size_t p = len; p > 0; --p)
+    if (buf[p - 1] == '\n') {
+      eff = p;
+      break;
+    }
+  unsigned nt = std::thread::hardware_concurrency();
+  if (nt == 0) nt = 1;
+  nt = std::min<unsigned>(nt, 64);
+  nt = (unsigned)std::min<size_t>(nt, eff / (1 << 20) + 1);
+  std::vector<Chunk> ch(nt);
+  // chunk boundaries at line starts
+  size_t prev = 0;
+  for (unsigned c = 0; c < nt; ++c) {
+    size_t target = (c + 1 == nt) ? eff : (eff / nt) * (c + 1);
+    if (target < prev) target = prev;
+    while (target < eff && target > 0 && buf[target - 1] != '\n') ++target;
+    ch[c].begin = prev;
+    ch[c].end = target;
+    prev = target;
+  }
+  auto count = [&](unsigned c) {
+    uint64_t n = 0;
+    const char *p = buf + ch[c].begin, *e = buf + ch[c].end;
+    while (p < e) {
+      const void *q = memchr(p, '\n', (size_t)(e - p));
+      if (!q) break;
+      ++n;
+      p = (const char *)q + 1;
+    }
+    ch[c].lines = n;
+  };
+  {
+    std::vector<std::thread> th;
+    for (unsigned c = 1; c < nt; ++c) th.emplace_back(count, c);
+    count(0);
+    for (auto &x : th) x.join();
+  }
+  uint64_t nnz = 0;
+  for (auto &c : ch) {
+    c.first_line = nnz;
+    nnz += c.lines;
+  }
+  out->N = N;
+  out->dtype = dtype;
+  out->nnz = nnz;
+  for (int n = 0; n < N; ++n) out->idx[n].assign(nnz, 0);
+  if (dtype == GTK_F32)
+    out->vf.assign(nnz, 0.f);
+  else
+    out->vd.assign(nnz, 0.0);
+  std::vector<unsigned char> missing(nnz, 0);
+
+  auto work = [&](unsigned c) {
+    Chunk &k = ch[c];
+    const char *p = buf + k.begin, *e = buf + k.end;
+    uint64_t line = k.first_line;
+    std::string vtok;
+    while (p < e) {
+      const char *nl = (const char *)memchr(p, '\n', (size_t)(e - p));
+      if (!nl) break;
+      const char *s = p;
+      int n = 0;
+      const char *vs = nullptr, *ve = nullptr;
+      while (s < nl) {
+        while (s < nl && is_delim(*s)) ++s;
+        if (s >= nl) break;
+        const char *te = s;
+        while (te < nl && !is_delim(*te)) ++te;
+        if (n < N) {
+          uint32_t v = parse_index(s, te);
+          if (v < 1) {
+            if (line < k.err_line) {
+              k.err_line = line;
+              k.err_code = GTK_ERR_PARSE;
+              k.err_msg = "input tensors must follow base-1 indexing";
+            }
+          } else {
+            out->idx[n][line] = v - 1;
+            if (v > k.maxd[n]) k.maxd[n] = v;
+          }
+          ++n;
+        } else {
+          vs = s;
+          ve = te;
+          break;
+        }
+        s = te;
+      }
+      if (n < N) {
+        if (line < k.err_line) {
+          k.err_line = line;
+          k.err_code = GTK_ERR_PARSE;
+          k.err_msg = "line has fewer indices than the tensor order";
+        }
+      } else if (vs) {
+        vtok.assign(vs, ve);
+        char *endp = nullptr;
+        double d = strtod(vtok.c_str(), &endp);
+        if (endp == vtok.c_str()) {
+          if (line < k.err_line) {
+            k.err_line = line;
+            k.err_code = GTK_ERR_PARSE;
+            k.err_msg = "value token is not a number";
+          }
+        } else if (dtype == GTK_F32) {
+          out->vf[line] = (float)d;
+        } else {
+          out->vd[line] = d;
+        }
+      } else {
+        missing[line] = 1;
+      }
+      ++line;
+      p = nl + 1;
+    }
+  };
+  {
+    std::vector<std::thread> th;
+    for (unsigned c = 1; c < nt; ++c) th.emplace_back(work, c);
+    work(0);
+    for (auto &x : th) x.join();
+  }
+  for (auto &c : ch) {
+    if (c.err_code) {
+      char b[64];
+      snprintf(b, sizeof b, " (line %llu)", (unsigned long long)(c.err_line + 1));
+      return fail(c.err_code, c.err_msg + b);
+    }
+  }
+  for (int n = 0; n < N; ++n) {
+    out->dims[n] = 0;
+    for (auto &c : ch) out->dims[n] = std::max(out->dims[n], c.maxd[n]);
+  }
+  // values of lines without one, in file order
+  GlibcRand g(seed);
+  uint64_t draws = 0;
+  for (uint64_t l = 0; l < nnz; ++l) {
+    if (!missing[l]) continue;
+    if (dtype == GTK_F32)
+      out->vf[l] = g.frand01<float>();
+    else
+      out->vd[l] = g.frand01<double>();
+    ++draws;
+  }
+  out->draws = draws;
+  return 0;
+}
+
+int parse_file(const char *path, int N, int dtype, uint32_t seed, gtk_coo *out) {
+  FILE *f = fopen(path, "rb");
+  if (!f) return fail(GTK_ERR_IO, std::string("cannot open file \"") + path + "\" for reading");
+  std::vector<char> data;
+  if (fseek(f, 0, SEEK_END) == 0) {
+    long sz = ftell(f);
+    if (sz > 0) data.resize((size_t)sz);
+    fseek(f, 0, SEEK_SET);
+  }
+  size_t got = data.empty() ? 0 : fread(data.data(), 1, data.size(), f);
+  fclose(f);
+  if (got != data.size()) return fail(GTK_ERR_IO, std::string("short read on \"") + path + "\"");
+  return parse_buffer(data.data(), data.size(), N, dtype, seed, out);
+}
+
+}  // namespace gtk

@@ -1,0 +1,782 @@
+// sweep.cu -- the ALS mode update and the fit on the GPU (plain value_t form).
+//
+// Reference path being replaced (paths inside the GPUTucker project):
+//   delta ......... computing_delta_kernel, delta.cuh:33-92.  Per nonzero x at
+//                   (i_1..i_N): delta_j = sum over core entries g with g_n = j of
+//                   G[g] * prod_{k != n} A_k[i_k, g_k] (J^N terms, summed in core order)
+//   B, C .......... ComputingBC, update.cuh:35-101 (host, OpenMP, double):
+//                   B_r = lambda*I + sum delta delta^T, C_r = sum x*delta over row r
+//   row solve ..... update.cuh:163-194 (host, Eigen inverse): a_r = C_r^T B_r^-1
+//   fit ........... ComputingReconstructionKernel reconstruction.cuh:32-83 and the
+//                   error loop :259-276
+//
+// GB300 design:
+//   * The tensor is HBM-resident; mode n runs over the mode-n view (nonzeros
+//     stably sorted by global row i_n), so one factor row's nonzeros are
+//     contiguous.
+//   * One fused kernel per mode: a CTA takes a tile of 256*NPT consecutive
+//     nonzeros, gathers the other modes' factor rows (L2-resident), contracts
+//     the mode-n-first permuted core G_n (in shared memory, broadcast reads)
+//     level by level -- J^N + J^(N-1) + ... + J^2 multiply-adds per nonzero
+//     instead of the reference's (N-1) J^N -- writes delta and x to a shared
+//     tile, and reduces delta delta^T (upper triangle) and x*delta per row
+//     segment of the tile.  delta never reaches HBM.  Rows wholly inside a tile
+//     are stored, rows cut by a tile edge are added with FP64 atomics.
+//   * One warp per row solves (lambda I + Gram) a = C by Cholesky in FP64.
+//   * The fit reuses the fused kernel on the last mode's view: x_hat =
+//     delta^(N-1) . a_{N-1}[i_{N-1}], error (x - x_hat)^2 summed in FP64 per
+//     CTA and then in a fixed order.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "internal.h"
+
+namespace gtk {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kFitGridMax = 1024;
+
+enum Kind { kUpdate = 0, kFit = 1, kDelta = 2 };
+
+template <int B, int E> struct Pow { static constexpr int v = B * Pow<B, E - 1>::v; };
+template <int B> struct Pow<B, 0> { static constexpr int v = 1; };
+
+struct ModeArgs {
+  const uint32_t *coord[kMaxOrder];  // view coordinates (global), coord[mode] = row
+  const void *val;                   // view values
+  const void *fac[kMaxOrder];        // factor matrices, row stride ldf
+  const void *corep;                 // [J^(N-1)][ldf], mode first
+  const uint32_t *vperm;             // view -> block-major position (kDelta)
+  void *out;                         // kDelta: delta [nnz][J] block-major
+  double *gram;                      // kUpdate: [rows][E]
+  double *partial;                   // kFit: per-CTA error sums
+  uint64_t nnz;
+  int N, J, ldf, mode, E, ldd;
+  int others[kMaxOrder];             // the other modes in increasing order
+  uint64_t gp_elems;                 // J^(N-1) * ldf
+  int gp_in_smem;                    // generic kernel: core in shared memory?
+};
+
+// ---------------------------------------------------------------- vector loads
+template <class V> struct Vec;
+template <> struct Vec<float> {
+  using T = float4;
+  static constexpr int W = 4;
+  __device__ static void unpack(const T &v, float *o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+};
+template <> struct Vec<double> {
+  using T = double2;
+  static constexpr int W = 2;
+  __device__ static void unpack(const T &v, double *o) { o[0] = v.x; o[1] = v.y; }
+};
+
+// ---------------------------------------------------------------- contraction nest
+// Nest<D> contracts D other modes.  g: the core sub-block for the current outer
+// indices, J^(D-1) rows of LDG values.  The two innermost levels use factor rows
+// held in registers (a1: second-to-last other mode, a2: last); outer levels read
+// their factor rows from shared memory (arow, element (q, j) at arow[(q*J+j)*kThreads]).
+template <class V, int J, int LDG, int NPT, int D> struct Nest {
+  static __device__ __forceinline__ void run(const V *__restrict__ g, const V *arow, int lvl_stride,
+                                             const V (&a1)[NPT][J], const V (&a2)[NPT][J], V (&out)[NPT]) {
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) out[q] = V(0);
+#pragma unroll 1
+    for (int j = 0; j < J; ++j) {
+      V sub[NPT];
+      Nest<V, J, LDG, NPT, D - 1>::run(g + (size_t)j * Pow<J, D - 2>::v * LDG, arow + lvl_stride, lvl_stride, a1, a2,
+                                       sub);
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) out[q] += arow[(q * J + j) * kThreads] * sub[q];
+    }
+  }
+};
+
+template <class V, int J, int LDG, int NPT> struct Nest<V, J, LDG, NPT, 2> {
+  static __device__ __forceinline__ void run(const V *__restrict__ g, const V *, int, const V (&a1)[NPT][J],
+                                             const V (&a2)[NPT][J], V (&out)[NPT]) {
+    using VT = typename Vec<V>::T;
+    constexpr int W = Vec<V>::W;
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) out[q] = V(0);
+#pragma unroll
+    for (int j1 = 0; j1 < J; ++j1) {
+      V d[NPT];
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) d[q] = V(0);
+      const VT *row = reinterpret_cast<const VT *>(g + j1 * LDG);
+#pragma unroll
+      for (int c = 0; c < LDG / W; ++c) {
+        V gv[W];
+        Vec<V>::unpack(row[c], gv);
+#pragma unroll
+        for (int k = 0; k < W; ++k) {
+          if (c * W + k < J) {
+#pragma unroll
+            for (int q = 0; q < NPT; ++q) d[q] += gv[k] * a2[q][c * W + k];
+          }
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) out[q] += a1[q][j1] * d[q];
+    }
+  }
+};
+
+// ---------------------------------------------------------------- shared tile layout
+template <class V> struct TileSmem {
+  // carve: [gp][arow][dx][rows][seg_start][pairs]
+  V *gp;
+  V *arow;
+  V *dx;
+  uint32_t *rows;
+  uint32_t *seg;
+  unsigned char *pi, *pj;
+};
+
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Shared memory needed by a tile of `tn` nonzeros.
+inline size_t tile_smem_bytes(size_t vsize, size_t gp_elems, int arow_levels, int npt, int J, int ldd, int E,
+                              int tn) {
+  size_t b = align_up(gp_elems * vsize, 16);
+  b += align_up((size_t)arow_levels * npt * J * kThreads * vsize, 16);
+  b += align_up((size_t)tn * ldd * vsize, 16);
+  b += align_up((size_t)tn * 4, 16);
+  b += align_up((size_t)(tn + 1) * 4, 16);
+  b += align_up((size_t)E * 2, 16);
+  return b;
+}
+
+template <class V>
+__device__ TileSmem<V> carve(unsigned char *base, size_t gp_elems, int arow_levels, int npt, int J, int ldd, int E,
+                             int tn) {
+  TileSmem<V> s;
+  size_t off = 0;
+  s.gp = reinterpret_cast<V *>(base + off);
+  off += align_up(gp_elems * sizeof(V), 16);
+  s.arow = reinterpret_cast<V *>(base + off);
+  off += align_up((size_t)arow_levels * npt * J * kThreads * sizeof(V), 16);
+  s.dx = reinterpret_cast<V *>(base + off);
+  off += align_up((size_t)tn * ldd * sizeof(V), 16);
+  s.rows = reinterpret_cast<uint32_t *>(base + off);
+  off += align_up((size_t)tn * 4, 16);
+  s.seg = reinterpret_cast<uint32_t *>(base + off);
+  off += align_up((size_t)(tn + 1) * 4, 16);
+  s.pi = base + off;
+  s.pj = base + off + E;
+  return s;
+}
+
+// pair table of the Gram/RHS entries: e -> (i, j), i <= j <= J, except (J, J).
+// Column J of the delta tile holds x, so (i, J) is the right-hand side C_i.
+__device__ void fill_pairs(unsigned char *pi, unsigned char *pj, int J) {
+  if (threadIdx.x == 0) {
+    int e = 0;
+    for (int i = 0; i <= J; ++i)
+      for (int j = i; j <= J; ++j) {
+        if (i == J && j == J) continue;
+        pi[e] = (unsigned char)i;
+        pj[e] = (unsigned char)j;
+        ++e;
+      }
+  }
+}
+
+template <class V> struct Acc { using T = V; };
+
+// Row-segmented reduction of the tile into the FP64 Gram/RHS rows.
+// tile_start: view position of tile element 0; nv: valid elements in the tile.
+template <class V>
+__device__ void gram_phase(const ModeArgs &a, const TileSmem<V> &s, uint64_t tile_start, int nv, int npt) {
+  using A = typename Acc<V>::T;
+  const int tid = threadIdx.x;
+  __shared__ uint32_t sw[32];
+  __shared__ uint32_t nseg_s;
+  // segment heads over contiguous chunks of npt positions per thread
+  uint32_t cnt = 0;
+  for (int k = 0; k < npt; ++k) {
+    int t = tid * npt + k;
+    if (t < nv && (t == 0 || s.rows[t] != s.rows[t - 1])) ++cnt;
+  }
+  // block exclusive scan of cnt
+  {
+    const int lane = tid & 31, warp = tid >> 5;
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      uint32_t w = lane < (kThreads / 32) ? sw[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        if (lane >= o) w += y;
+      }
+      if (lane < kThreads / 32) sw[lane] = w;
+      if (lane == kThreads / 32 - 1) nseg_s = w;
+    }
+    __syncthreads();
+    uint32_t id = (warp > 0 ? sw[warp - 1] : 0u) + x - cnt;
+    for (int k = 0; k < npt; ++k) {
+      int t = tid * npt + k;
+      if (t < nv && (t == 0 || s.rows[t] != s.rows[t - 1])) s.seg[id++] = (uint32_t)t;
+    }
+    if (tid == 0) s.seg[nseg_s] = (uint32_t)nv;
+  }
+  __syncthreads();
+  const int nseg = (int)nseg_s;
+  const int E = a.E, ldd = a.ldd;
+  // does the tile hold the whole first / last row?
+  const uint32_t first_row = s.rows[0], last_row = nv > 0 ? s.rows[nv - 1] : 0u;
+  const bool first_open = tile_start > 0 && a.coord[a.mode][tile_start - 1] == first_row;
+  const bool last_open = tile_start + nv < a.nnz && a.coord[a.mode][tile_start + nv] == last_row;
+  const int items = nseg * E;
+  for (int w = tid; w < items; w += kThreads) {
+    const int sgi = w / E, e = w - sgi * E;
+    const int i = s.pi[e], j = s.pj[e];
+    const int t0 = (int)s.seg[sgi], t1 = (int)s.seg[sgi + 1];
+    A acc = A(0);
+    for (int t = t0; t < t1; ++t) acc += (A)s.dx[t * ldd + i] * (A)s.dx[t * ldd + j];
+    const uint32_t row = s.rows[t0];
+    double *dst = a.gram + (size_t)row * E + e;
+    const bool shared_row = (sgi == 0 && first_open) || (sgi == nseg - 1 && last_open);
+    if (shared_row)
+      atomicAdd(dst, (double)acc);
+    else
+      *dst = (double)acc;
+  }
+}
+
+
+__device__ inline double block_sum(double v) {
+  __shared__ double sw[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  if (lane == 0) sw[warp] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sw[w];
+  __syncthreads();
+  return s;  // valid in thread 0
+}
+
+// ---------------------------------------------------------------- specialised kernel
+// Compile-time order N and rank J; NPT nonzeros per thread share every core read.
+template <class V, int N, int J, int NPT, int KIND>
+__global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
+  using VT = typename Vec<V>::T;
+  constexpr int W = Vec<V>::W;
+  constexpr int LDG = (J + W - 1) / W * W;  // equals the factor row stride ldf
+  constexpr int D = N - 1;                 // other modes
+  constexpr int LEV = D > 2 ? D - 2 : 0;   // outer levels with factor rows in shared memory
+  constexpr int TN = kThreads * NPT;
+  constexpr size_t GP = (size_t)Pow<J, N - 1>::v * LDG;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const TileSmem<V> s = carve<V>(smem, GP, LEV, NPT, J, a.ldd, a.E, TN);
+  const int tid = threadIdx.x;
+  {
+    const VT *src = reinterpret_cast<const VT *>(a.corep);
+    VT *dst = reinterpret_cast<VT *>(s.gp);
+    for (size_t k = tid; k < GP / W; k += kThreads) dst[k] = src[k];
+  }
+  if (KIND == kUpdate) fill_pairs(s.pi, s.pj, J);
+  const int lvl_stride = NPT * J * kThreads;
+  const V *facn = reinterpret_cast<const V *>(a.fac[a.mode]);
+  double err = 0;
+  const uint64_t ntiles = (a.nnz + TN - 1) / TN;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    __syncthreads();  // previous tile's reduction is done with the shared tile
+    const uint64_t t0 = tile * TN;
+    const int nv = (int)min((uint64_t)TN, a.nnz - t0);
+    V a1[NPT][J], a2[NPT][J];
+    V xv[NPT];
+    uint32_t rowv[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) {
+      const int tl = q * kThreads + tid;
+      const bool valid = tl < nv;
+      const uint64_t gi = valid ? t0 + tl : t0;
+      rowv[q] = valid ? a.coord[a.mode][gi] : 0xFFFFFFFFu;
+      xv[q] = valid ? reinterpret_cast<const V *>(a.val)[gi] : V(0);
+#pragma unroll
+      for (int l = 0; l < D; ++l) {
+        const int o = a.others[l];
+        const uint32_t r = a.coord[o][gi];
+        const VT *frow = reinterpret_cast<const VT *>(reinterpret_cast<const V *>(a.fac[o]) + (size_t)r * LDG);
+        V tmp[LDG];
+#pragma unroll
+        for (int c = 0; c < LDG / W; ++c) Vec<V>::unpack(__ldg(frow + c), tmp + c * W);
+        if (l == D - 2) {
+#pragma unroll
+          for (int j = 0; j < J; ++j) a1[q][j] = tmp[j];
+        } else if (l == D - 1) {
+#pragma unroll
+          for (int j = 0; j < J; ++j) a2[q][j] = tmp[j];
+        } else {
+#pragma unroll
+          for (int j = 0; j < J; ++j) s.arow[l * lvl_stride + (q * J + j) * kThreads + tid] = tmp[j];
+        }
+      }
+    }
+    V xhat[NPT];
+#pragma unroll
+    for (int q = 0; q < NPT; ++q) xhat[q] = V(0);
+#pragma unroll 1
+    for (int jn = 0; jn < J; ++jn) {
+      V o[NPT];
+      Nest<V, J, LDG, NPT, D>::run(s.gp + (size_t)jn * Pow<J, N - 2>::v * LDG, s.arow + tid, lvl_stride, a1, a2, o);
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const int tl = q * kThreads + tid;
+        if (KIND == kUpdate) {
+          s.dx[tl * a.ldd + jn] = o[q];
+        } else if (KIND == kFit) {
+          if (tl < nv) xhat[q] += o[q] * __ldg(facn + (size_t)rowv[q] * LDG + jn);
+        } else {
+          if (tl < nv) reinterpret_cast<V *>(a.out)[(size_t)a.vperm[t0 + tl] * J + jn] = o[q];
+        }
+      }
+    }
+    if (KIND == kUpdate) {
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        const int tl = q * kThreads + tid;
+        s.dx[tl * a.ldd + J] = xv[q];
+        s.rows[tl] = rowv[q];
+      }
+      __syncthreads();
+      gram_phase<V>(a, s, t0, nv, NPT);
+    } else if (KIND == kFit) {
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) {
+        if (q * kThreads + tid < nv) {
+          const V d = xv[q] - xhat[q];
+          err += (double)d * (double)d;
+        }
+      }
+    }
+  }
+  if (KIND == kFit) {
+    const double tot = block_sum(err);
+    if (tid == 0) a.partial[blockIdx.x] = tot;
+  }
+}
+
+// ---------------------------------------------------------------- generic kernel
+// Any order N (1..8) and rank J (1..64); one nonzero per thread; the core is read
+// from shared memory when it fits, else from global memory (L1/L2).  delta_jn =
+// sum over rows r of G_n[jn][r][:] . a_last * prod of the outer factor entries.
+template <class V, int KIND>
+__global__ void __launch_bounds__(kThreads) k_mode_gen(ModeArgs a) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const size_t gp_sm = a.gp_in_smem ? a.gp_elems : 0;
+  const TileSmem<V> s = carve<V>(smem, gp_sm, 0, 1, a.J, a.ldd, a.E, kThreads);
+  const int tid = threadIdx.x;
+  const int J = a.J, ldf = a.ldf, M = a.N - 1;
+  const V *gp = reinterpret_cast<const V *>(a.corep);
+  if (a.gp_in_smem) {
+    for (size_t k = tid; k < a.gp_elems; k += kThreads) s.gp[k] = gp[k];
+    gp = s.gp;
+  }
+  if (KIND == kUpdate) fill_pairs(s.pi, s.pj, J);
+  uint64_t rows_per = 1;
+  for (int k = 0; k < M - 1; ++k) rows_per *= (uint64_t)J;
+  const V *facn = reinterpret_cast<const V *>(a.fac[a.mode]);
+  double err = 0;
+  const uint64_t ntiles = (a.nnz + kThreads - 1) / kThreads;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    __syncthreads();
+    const uint64_t t0 = tile * kThreads;
+    const int nv = (int)min((uint64_t)kThreads, a.nnz - t0);
+    const bool valid = tid < nv;
+    const uint64_t gi = valid ? t0 + tid : t0;
+    const uint32_t row = valid ? a.coord[a.mode][gi] : 0xFFFFFFFFu;
+    const V x = valid ? reinterpret_cast<const V *>(a.val)[gi] : V(0);
+    const V *ap[kMaxOrder];
+    for (int k = 0; k < M; ++k) {
+      const int o = a.others[k];
+      ap[k] = reinterpret_cast<const V *>(a.fac[o]) + (size_t)a.coord[o][gi] * ldf;
+    }
+    V xhat = V(0);
+    for (int jn = 0; jn < J; ++jn) {
+      V acc = V(0);
+      if (M == 0) {
+        acc = gp[jn];
+      } else {
+        int dig[kMaxOrder];
+        for (int k = 0; k < M; ++k) dig[k] = 0;
+        const V *alast = ap[M - 1];
+        for (uint64_t r = 0; r < rows_per; ++r) {
+          V pp = V(1);
+          for (int k = 0; k < M - 1; ++k) pp *= ap[k][dig[k]];
+          const V *grow = gp + ((size_t)jn * rows_per + r) * ldf;
+          V dot = V(0);
+          for (int c = 0; c < J; ++c) dot += grow[c] * alast[c];
+          acc += pp * dot;
+          for (int k = M - 2; k >= 0; --k) {
+            if (++dig[k] < J) break;
+            dig[k] = 0;
+          }
+        }
+      }
+      if (KIND == kUpdate) {
+        s.dx[tid * a.ldd + jn] = acc;
+      } else if (KIND == kFit) {
+        if (valid) xhat += acc * facn[(size_t)row * ldf + jn];
+      } else {
+        if (valid) reinterpret_cast<V *>(a.out)[(size_t)a.vperm[gi] * J + jn] = acc;
+      }
+    }
+    if (KIND == kUpdate) {
+      s.dx[tid * a.ldd + J] = x;
+      s.rows[tid] = row;
+      __syncthreads();
+      gram_phase<V>(a, s, t0, nv, 1);
+    } else if (KIND == kFit) {
+      if (valid) {
+        const V d = x - xhat;
+        err += (double)d * (double)d;
+      }
+    }
+  }
+  if (KIND == kFit) {
+    const double tot = block_sum(err);
+    if (tid == 0) a.partial[blockIdx.x] = tot;
+  }
+}
+
+// ---------------------------------------------------------------- row solves
+// One warp per factor row: A = lambda I + Gram (FP64), Cholesky A = L L^T in
+// shared memory, L y = C, L^T a = y; a (cast to value_t) overwrites the row.
+// A non-positive pivot sets bit 0 of *status (the reference's Eigen inverse
+// would return inf/nan there); the row is still written.
+template <class V>
+__global__ void k_solve(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf, V *__restrict__ fac,
+                        int *__restrict__ status, double lambda) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  double *A = sm + (size_t)wib * ((size_t)J * J + J);
+  double *b = A + (size_t)J * J;
+  for (uint64_t row = (uint64_t)blockIdx.x * wpb + wib; row < rows; row += (uint64_t)gridDim.x * wpb) {
+    const double *g = gram + row * (uint64_t)E;
+    for (int e = lane; e < E; e += 32) {
+      int i = 0, off = 0;
+      while (off + (J + 1 - i) <= e) {
+        off += J + 1 - i;
+        ++i;
+      }
+      const int j = i + (e - off);
+      const double v = g[e];
+      if (j == J) {
+        b[i] = v;
+      } else {
+        A[i * J + j] = v;
+        A[j * J + i] = v;
+      }
+    }
+    __syncwarp();
+    for (int i = lane; i < J; i += 32) A[i * J + i] += lambda;
+    __syncwarp();
+    for (int k = 0; k < J; ++k) {
+      double d = A[k * J + k];
+      const bool bad = !(d > 0.0) || !isfinite(d);
+      if (bad) d = 1e-300;
+      const double lkk = sqrt(d);
+      __syncwarp();
+      for (int i = k + 1 + lane; i < J; i += 32) A[i * J + k] /= lkk;
+      if (lane == 0) {
+        A[k * J + k] = lkk;
+        if (bad) atomicOr(status, 1);
+      }
+      __syncwarp();
+      for (int i = k + 1 + lane; i < J; i += 32) {
+        const double lik = A[i * J + k];
+        for (int j = k + 1; j <= i; ++j) A[i * J + j] -= lik * A[j * J + k];
+      }
+      __syncwarp();
+    }
+    for (int k = 0; k < J; ++k) {
+      const double yk = b[k] / A[k * J + k];
+      __syncwarp();
+      if (lane == 0) b[k] = yk;
+      for (int i = k + 1 + lane; i < J; i += 32) b[i] -= A[i * J + k] * yk;
+      __syncwarp();
+    }
+    for (int k = J - 1; k >= 0; --k) {
+      const double ak = b[k] / A[k * J + k];
+      __syncwarp();
+      if (lane == 0) b[k] = ak;
+      for (int i = lane; i < k; i += 32) b[i] -= A[k * J + i] * ak;
+      __syncwarp();
+    }
+    V *frow = fac + row * (uint64_t)ldf;
+    for (int j = lane; j < ldf; j += 32) frow[j] = j < J ? (V)b[j] : V(0);
+    __syncwarp();
+  }
+}
+
+__global__ void k_sum_fit(const double *__restrict__ partial, int m, double *__restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 0;
+    for (int i = 0; i < m; ++i) s += partial[i];
+    *out = s;
+  }
+}
+
+// ---------------------------------------------------------------- dispatch
+struct Launch {
+  const void *fn = nullptr;
+  size_t smem = 0;
+  int tn = 0;  // nonzeros per tile
+  bool spec = false;
+};
+
+inline int ldd_for(int J) { return ((J + 1) & 1) ? J + 1 : J + 2; }
+inline int pairs_for(int J) { return (J + 1) * (J + 2) / 2 - 1; }
+
+template <class V, int N, int J, int KIND> void spec_entry(Launch &L, const DevTensor &t) {
+  constexpr int NPT = 2;
+  constexpr int W = Vec<V>::W;
+  constexpr int LDG = (J + W - 1) / W * W;
+  constexpr int D = N - 1;
+  constexpr int LEV = D > 2 ? D - 2 : 0;
+  const size_t gp = (size_t)Pow<J, N - 1>::v * LDG;
+  L.fn = (const void *)k_mode_spec<V, N, J, NPT, KIND>;
+  L.smem = tile_smem_bytes(sizeof(V), gp, LEV, NPT, J, ldd_for(J), pairs_for(J), kThreads * NPT);
+  L.tn = kThreads * NPT;
+  L.spec = true;
+  (void)t;
+}
+
+// The specialised (N, J) table.  Anything else runs the generic kernel.
+template <class V, int KIND> bool find_spec(Launch &L, const DevTensor &t) {
+#define GTK_SPEC(NN, JJ)                                          \
+  if (t.N == NN && t.J == JJ) {                                   \
+    spec_entry<V, NN, JJ, KIND>(L, t);                            \
+    return true;                                                  \
+  }
+  GTK_SPEC(3, 4) GTK_SPEC(3, 8) GTK_SPEC(3, 10) GTK_SPEC(3, 12) GTK_SPEC(3, 16)
+  GTK_SPEC(4, 4) GTK_SPEC(4, 8) GTK_SPEC(4, 10) GTK_SPEC(4, 12)
+  GTK_SPEC(5, 4) GTK_SPEC(5, 8)
+#undef GTK_SPEC
+  return false;
+}
+
+constexpr size_t kSmemLimit = 227 * 1024;
+
+template <class V, int KIND> int choose(Launch &L, const DevTensor &t, bool &gp_in_smem) {
+  gp_in_smem = true;
+  if (find_spec<V, KIND>(L, t) && L.smem <= kSmemLimit) return 0;
+  const size_t gp = (size_t)t.core_n / (size_t)t.J * t.ldf;
+  L.spec = false;
+  L.tn = kThreads;
+  L.fn = (const void *)k_mode_gen<V, KIND>;
+  L.smem = tile_smem_bytes(sizeof(V), gp, 0, 1, t.J, ldd_for(t.J), pairs_for(t.J), kThreads);
+  if (L.smem > 160 * 1024) {
+    gp_in_smem = false;
+    L.smem = tile_smem_bytes(sizeof(V), 0, 0, 1, t.J, ldd_for(t.J), pairs_for(t.J), kThreads);
+  }
+  return 0;
+}
+
+int prepare_fn(const void *fn, size_t smem) {
+  static std::vector<std::pair<const void *, size_t>> done;
+  for (auto &d : done)
+    if (d.first == fn && d.second >= smem) return 0;
+  GTK_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  done.emplace_back(fn, smem);
+  return 0;
+}
+
+ModeArgs make_args(const DevTensor &t, int mode) {
+  ModeArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int k = 0; k < t.N; ++k) {
+    a.coord[k] = t.vidx[mode][k];
+    a.fac[k] = t.fac[k];
+  }
+  a.val = t.vval[mode];
+  a.corep = t.corep[mode];
+  a.vperm = t.vperm[mode];
+  a.gram = t.gram;
+  a.partial = t.partial;
+  a.nnz = t.nnz;
+  a.N = t.N;
+  a.J = t.J;
+  a.ldf = t.ldf;
+  a.mode = mode;
+  a.E = pairs_for(t.J);
+  a.ldd = ldd_for(t.J);
+  int m = 0;
+  for (int k = 0; k < t.N; ++k)
+    if (k != mode) a.others[m++] = k;
+  a.gp_elems = (uint64_t)(t.core_n / (uint64_t)t.J) * (uint64_t)t.ldf;
+  return a;
+}
+
+// profiling scopes: events recorded around a launch, resolved on read
+struct ProfEvent {
+  int kind;
+  cudaEvent_t a, b;
+};
+std::vector<ProfEvent> &pending_events() {
+  static std::vector<ProfEvent> v;
+  return v;
+}
+
+}  // namespace
+
+// record helpers used by the launch sites below and by api.cpp
+int prof_begin(DevTensor &t, cudaEvent_t *a) {
+  if (!t.prof) return 0;
+  GTK_CUDA(cudaEventCreate(a));
+  GTK_CUDA(cudaEventRecord(*a, t.stream));
+  return 0;
+}
+int prof_end(DevTensor &t, int kind, cudaEvent_t a) {
+  if (!t.prof) return 0;
+  cudaEvent_t b;
+  GTK_CUDA(cudaEventCreate(&b));
+  GTK_CUDA(cudaEventRecord(b, t.stream));
+  pending_events().push_back({kind, a, b});
+  return 0;
+}
+int prof_resolve(DevTensor &t) {
+  auto &v = pending_events();
+  if (v.empty()) return 0;
+  GTK_CUDA(cudaStreamSynchronize(t.stream));
+  for (auto &e : v) {
+    float ms = 0;
+    GTK_CUDA(cudaEventElapsedTime(&ms, e.a, e.b));
+    t.prof_ms[e.kind] += ms;
+    t.prof_n[e.kind] += 1;
+    cudaEventDestroy(e.a);
+    cudaEventDestroy(e.b);
+  }
+  v.clear();
+  return 0;
+}
+
+template <class V, int KIND> static int launch_mode(DevTensor &t, int mode, void *out, int *grid_out) {
+  Launch L;
+  bool gp_in_smem = true;
+  choose<V, KIND>(L, t, gp_in_smem);
+  if (int rc = prepare_fn(L.fn, L.smem)) return rc;
+  ModeArgs a = make_args(t, mode);
+  a.gp_in_smem = gp_in_smem ? 1 : 0;
+  a.out = out;
+  int per_sm = 0;
+  GTK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, kThreads, L.smem));
+  if (per_sm < 1) return fail(GTK_ERR_UNSUPPORTED, "mode kernel does not fit on an SM");
+  const uint64_t ntiles = (t.nnz + L.tn - 1) / L.tn;
+  uint64_t grid = std::min<uint64_t>(ntiles, (uint64_t)per_sm * t.num_sms);
+  if (KIND == kFit) grid = std::min<uint64_t>(grid, kFitGridMax);
+  if (grid < 1) grid = 1;
+  void *args[] = {&a};
+  GTK_CUDA(cudaLaunchKernel(L.fn, dim3((unsigned)grid), dim3(kThreads), args, L.smem, t.stream));
+  if (grid_out) *grid_out = (int)grid;
+  return 0;
+}
+
+template <class V> static int update_impl(DevTensor &t, int mode) {
+  const int E = pairs_for(t.J);
+  cudaEvent_t ev = nullptr;
+  if (int rc = prof_begin(t, &ev)) return rc;
+  GTK_CUDA(cudaMemsetAsync(t.gram, 0, t.rows[mode] * (uint64_t)E * 8, t.stream));
+  if (t.nnz) {
+    if (int rc = launch_mode<V, kUpdate>(t, mode, nullptr, nullptr)) return rc;
+  }
+  if (int rc = prof_end(t, 0, ev)) return rc;
+  if (int rc = prof_begin(t, &ev)) return rc;
+  const int J = t.J;
+  const size_t per_warp = ((size_t)J * J + J) * 8;
+  int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (48 * 1024) / per_warp));
+  const size_t smem = per_warp * wpb;
+  if (int rc = prepare_fn((const void *)k_solve<V>, smem)) return rc;
+  uint64_t grid = (t.rows[mode] + wpb - 1) / wpb;
+  grid = std::min<uint64_t>(grid, (uint64_t)t.num_sms * 32);
+  if (grid < 1) grid = 1;
+  k_solve<V><<<(unsigned)grid, wpb * 32, smem, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf, (V *)t.fac[mode],
+                                                           t.status, kLambda);
+  GTK_CUDA(cudaGetLastError());
+  if (int rc = prof_end(t, 1, ev)) return rc;
+  return 0;
+}
+
+int run_update_mode(DevTensor &t, int mode) {
+  return t.dtype == GTK_F32 ? update_impl<float>(t, mode) : update_impl<double>(t, mode);
+}
+
+template <class V> static int fit_impl(DevTensor &t, double *fit) {
+  cudaEvent_t ev = nullptr;
+  if (int rc = prof_begin(t, &ev)) return rc;
+  int grid = 1;
+  if (t.nnz) {
+    if (int rc = launch_mode<V, kFit>(t, t.N - 1, nullptr, &grid)) return rc;
+  } else {
+    GTK_CUDA(cudaMemsetAsync(t.partial, 0, 8, t.stream));
+  }
+  k_sum_fit<<<1, 32, 0, t.stream>>>(t.partial, grid, t.partial + kFitGridMax);
+  GTK_CUDA(cudaGetLastError());
+  if (int rc = prof_end(t, 2, ev)) return rc;
+  double err = 0;
+  GTK_CUDA(cudaMemcpyAsync(&err, t.partial + kFitGridMax, 8, cudaMemcpyDeviceToHost, t.stream));
+  GTK_CUDA(cudaStreamSynchronize(t.stream));
+  *fit = (t.norm == 0) ? 1.0 : 1.0 - std::sqrt(err) / t.norm;
+  return 0;
+}
+
+int run_fit(DevTensor &t, double *fit) { return t.dtype == GTK_F32 ? fit_impl<float>(t, fit) : fit_impl<double>(t, fit); }
+
+int run_delta(DevTensor &t, int mode, void *d_out) {
+  if (!t.nnz) return 0;
+  return t.dtype == GTK_F32 ? launch_mode<float, kDelta>(t, mode, d_out, nullptr)
+                            : launch_mode<double, kDelta>(t, mode, d_out, nullptr);
+}
+
+// Builds G_n (mode n first, the other modes in increasing order, the last one
+// fastest, rows padded to ldf) for every mode and uploads them.
+int upload_core_perms(DevTensor &t, const void *core_host) {
+  const int N = t.N, J = t.J, ldf = t.ldf;
+  const uint64_t rows = t.core_n / (uint64_t)J;
+  std::vector<unsigned char> buf(rows * ldf * t.vsize);
+  for (int n = 0; n < N; ++n) {
+    std::fill(buf.begin(), buf.end(), 0);
+    int others[kMaxOrder], m = 0;
+    for (int k = 0; k < N; ++k)
+      if (k != n) others[m++] = k;
+    for (uint64_t L = 0; L < t.core_n; ++L) {
+      // digits of L over (n, others...) with the last fastest
+      uint64_t rem = L, lin = 0;
+      uint32_t dig[kMaxOrder];
+      for (int k = N - 1; k >= 0; --k) {
+        dig[k] = (uint32_t)(rem % J);
+        rem /= J;
+      }
+      uint32_t full[kMaxOrder];
+      full[n] = dig[0];
+      for (int k = 0; k < m; ++k) full[others[k]] = dig[k + 1];
+      for (int k = 0; k < N; ++k) lin = lin * J + full[k];
+      const uint64_t row = L / J, col = L % J;
+      memcpy(&buf[(row * ldf + col) * t.vsize], (const unsigned char *)core_host + lin * t.vsize, t.vsize);
+    }
+    GTK_CUDA(cudaMemcpyAsync(t.corep[n], buf.data(), buf.size(), cudaMemcpyHostToDevice, t.stream));
+    GTK_CUDA(cudaStreamSynchronize(t.stream));
+  }
+  return 0;
+}
+
+}  // namespace gtk

@@ -1,0 +1,320 @@
+"""Host-side API mirroring GPUTucker's interface for the factor-update path.
+
+Reference interface (paths inside the GPUTucker project) -> this module:
+
+    ParseFromFile(path, &tensor)            tensor_manager.tpp:19   -> parse_from_file
+    CreateTensorBlocks(&src, &dst, opt)     tensor_manager.tpp:201  -> create_tensor_blocks
+    init of factors/core in TuckerDecomposition  tucker.cuh:71-134  -> BlockedTensor.init_random
+    UpdateFactorMatrices(...)               update.cuh:128          -> BlockedTensor.update_factor_matrices
+    Reconstruction(..., &fit, ...)          reconstruction.cuh:228  -> BlockedTensor.reconstruction
+    TuckerDecomposition(tensor, rank, gpus) tucker.cuh:30           -> tucker_decomposition
+
+Every call goes through the C ABI of libgputucker_gb300.so (include/gputucker_gb300.h);
+the arithmetic runs in that library's CUDA kernels.  Arrays cross as numpy
+arrays in the reference's layouts (factor n = its slabs stacked, [P_n*block_dims[n], J]).
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as nat
+from ._native import call
+
+_DT = {"f32": nat.GTK_F32, "f64": nat.GTK_F64, np.float32: nat.GTK_F32, np.float64: nat.GTK_F64}
+_NP = {nat.GTK_F32: np.float32, nat.GTK_F64: np.float64}
+
+
+def _dtype_code(dtype) -> int:
+    if isinstance(dtype, int):
+        return dtype
+    if isinstance(dtype, np.dtype):
+        dtype = dtype.type
+    return _DT[dtype]
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class Coo:
+    """A parsed tensor held on the host (one block, global 0-based coordinates)."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        lib = nat.load()
+        order, dtype, nnz, draws = C.c_int(), C.c_int(), C.c_uint64(), C.c_uint64()
+        dims = (C.c_uint32 * nat.GTK_MAX_ORDER)()
+        nat.check(lib.gtk_coo_info(handle, C.byref(order), C.byref(dtype), C.byref(nnz), dims, C.byref(draws)))
+        self.order = order.value
+        self.dtype = dtype.value
+        self.nnz = nnz.value
+        self.dims = [dims[i] for i in range(self.order)]
+        self.rand_draws = draws.value
+
+    @property
+    def handle(self) -> C.c_void_p:
+        if self._h is None:
+            raise ValueError("Coo already freed")
+        return self._h
+
+    def arrays(self) -> tuple[list[np.ndarray], np.ndarray]:
+        idx = [np.empty(self.nnz, np.uint32) for _ in range(self.order)]
+        vals = np.empty(self.nnz, _NP[self.dtype])
+        ptrs = (C.c_void_p * self.order)(*[a.ctypes.data for a in idx])
+        call("gtk_coo_export", self.handle, ptrs, _ptr(vals))
+        return idx, vals
+
+    def pin(self) -> None:
+        """Page-lock the host arrays (cudaHostRegister) for full-speed uploads."""
+        call("gtk_coo_pin", self.handle)
+
+    def write_text(self, path: str) -> None:
+        call("gtk_write_text", self.handle, str(path).encode())
+
+    def free(self) -> None:
+        if self._h is not None:
+            nat.load().gtk_coo_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+def parse_from_file(path: str, order: int, dtype="f64", rand_seed: int = 1) -> Coo:
+    """The reference's text format (tensor_manager.tpp:19-191); see gtk_parse_file."""
+    h = C.c_void_p()
+    call("gtk_parse_file", str(path).encode(), order, _dtype_code(dtype), rand_seed, C.byref(h))
+    return Coo(h)
+
+
+def parse_buffer(data: bytes, order: int, dtype="f64", rand_seed: int = 1) -> Coo:
+    h = C.c_void_p()
+    call("gtk_parse_buffer", data, len(data), order, _dtype_code(dtype), rand_seed, C.byref(h))
+    return Coo(h)
+
+
+def coo_from_arrays(indices, values: np.ndarray, dims=None) -> Coo:
+    """COO from 0-based coordinate arrays (one per mode) and values (float32/float64)."""
+    values = np.ascontiguousarray(values)
+    code = _dtype_code(values.dtype)
+    idx = [np.ascontiguousarray(i, dtype=np.uint32) for i in indices]
+    order = len(idx)
+    ptrs = (C.c_void_p * order)(*[a.ctypes.data for a in idx])
+    d = None
+    if dims is not None:
+        d = np.ascontiguousarray(dims, dtype=np.uint32)
+    h = C.c_void_p()
+    call("gtk_coo_from_arrays", order, len(values), ptrs, _ptr(values), code,
+         _ptr(d) if d is not None else None, C.byref(h))
+    return Coo(h)
+
+
+def generate(order: int, dims, nnz: int, index_dist: str = "zipf", zipf_s: float = 1.1,
+             value_dist: str = "uniform", dtype="f32", seed: int = 0) -> Coo:
+    """Seeded synthetic tensor with distinct coordinates (gtk_generate)."""
+    d = np.ascontiguousarray(dims, dtype=np.uint32)
+    idist = {"uniform": nat.GTK_GEN_UNIFORM, "zipf": nat.GTK_GEN_ZIPF}[index_dist]
+    vdist = {"uniform": nat.GTK_VAL_UNIFORM, "lognormal": nat.GTK_VAL_LOGNORMAL}[value_dist]
+    h = C.c_void_p()
+    call("gtk_generate", order, d.ctypes.data_as(nat.U32P), nnz, idist, zipf_s, vdist, _dtype_code(dtype), seed,
+         C.byref(h))
+    return Coo(h)
+
+
+def generate_planted(order: int, dims, nnz: int, planted_rank: int, noise_sigma: float, dtype="f32",
+                     seed: int = 0) -> Coo:
+    d = np.ascontiguousarray(dims, dtype=np.uint32)
+    h = C.c_void_p()
+    call("gtk_generate_planted", order, d.ctypes.data_as(nat.U32P), nnz, planted_rank, noise_sigma,
+         _dtype_code(dtype), seed, C.byref(h))
+    return Coo(h)
+
+
+@dataclass
+class Info:
+    order: int
+    rank: int
+    dtype: int
+    device: int
+    nnz: int
+    block_count: int
+    dims: list
+    partition_dims: list
+    block_dims: list
+    norm: float
+    device_bytes: int
+
+
+class BlockedTensor:
+    """A blocked sparse tensor with its factor matrices and core, resident on one GPU."""
+
+    def __init__(self, handle: C.c_void_p):
+        self._h = handle
+        self.info = self._info()
+        self.order = self.info.order
+        self.rank = self.info.rank
+        self.np_dtype = _NP[self.info.dtype]
+
+    @property
+    def handle(self) -> C.c_void_p:
+        if self._h is None:
+            raise ValueError("tensor already destroyed")
+        return self._h
+
+    def _info(self) -> Info:
+        ti = nat.TensorInfo()
+        call("gtk_tensor_info_get", self._h, C.byref(ti))
+        n = ti.order
+        return Info(ti.order, ti.rank, ti.dtype, ti.device, ti.nnz, ti.block_count, list(ti.dims[:n]),
+                    list(ti.partition_dims[:n]), list(ti.block_dims[:n]), ti.norm, ti.device_bytes)
+
+    # ---- partition readback (bit-exact with the reference's blocks)
+    def block(self, b: int):
+        """(block coordinate, block-local coords per mode, values) of block b."""
+        coord = (C.c_uint32 * self.order)()
+        nnz = C.c_uint64()
+        call("gtk_block_info", self.handle, b, coord, C.byref(nnz))
+        n = nnz.value
+        idx = [np.empty(n, np.uint32) for _ in range(self.order)]
+        vals = np.empty(n, self.np_dtype)
+        ptrs = (C.c_void_p * self.order)(*[a.ctypes.data for a in idx])
+        call("gtk_block_data", self.handle, b, ptrs, _ptr(vals))
+        return list(coord), idx, vals
+
+    def segments(self, b: int, mode: int):
+        """(count_nnz, where_nnz) of block b for `mode` (block.tpp:115-186)."""
+        _, nnz = self.block_nnz(b)
+        cnt = np.empty(self.info.block_dims[mode] + 1, np.uint64)
+        where = np.empty(nnz, np.uint32)
+        call("gtk_block_segments", self.handle, b, mode, _ptr(cnt), _ptr(where))
+        return cnt, where
+
+    def block_nnz(self, b: int):
+        coord = (C.c_uint32 * self.order)()
+        nnz = C.c_uint64()
+        call("gtk_block_info", self.handle, b, coord, C.byref(nnz))
+        return list(coord), nnz.value
+
+    # ---- factors and core
+    def init_random(self, rand_seed: int = 1, skip_draws: int = 0) -> None:
+        call("gtk_init_random", self.handle, rand_seed, skip_draws)
+
+    def factor_rows(self, mode: int) -> int:
+        return self.info.partition_dims[mode] * self.info.block_dims[mode]
+
+    def get_factor(self, mode: int) -> np.ndarray:
+        a = np.empty((self.factor_rows(mode), self.rank), self.np_dtype)
+        call("gtk_get_factor", self.handle, mode, _ptr(a))
+        return a
+
+    def set_factor(self, mode: int, a: np.ndarray) -> None:
+        a = np.ascontiguousarray(a, dtype=self.np_dtype)
+        if a.shape != (self.factor_rows(mode), self.rank):
+            raise ValueError(f"factor {mode} must have shape {(self.factor_rows(mode), self.rank)}")
+        call("gtk_set_factor", self.handle, mode, _ptr(a))
+
+    def get_core(self) -> np.ndarray:
+        g = np.empty((self.rank,) * self.order, self.np_dtype)
+        call("gtk_get_core", self.handle, _ptr(g))
+        return g
+
+    def set_core(self, g: np.ndarray) -> None:
+        g = np.ascontiguousarray(g, dtype=self.np_dtype)
+        if g.size != self.rank ** self.order:
+            raise ValueError("core must have J^N entries")
+        call("gtk_set_core", self.handle, _ptr(g))
+
+    # ---- the sweep
+    def set_precision(self, precision: str) -> None:
+        code = {"plain": nat.GTK_PREC_PLAIN, "bf16": nat.GTK_PREC_BF16, "tf32": nat.GTK_PREC_TF32}[precision]
+        call("gtk_set_precision", self.handle, code)
+
+    def update_mode(self, mode: int) -> None:
+        call("gtk_update_mode", self.handle, mode)
+
+    def update_factor_matrices(self) -> None:
+        call("gtk_update_factor_matrices", self.handle)
+
+    def reconstruction(self) -> float:
+        f = C.c_double()
+        call("gtk_reconstruction", self.handle, C.byref(f))
+        return f.value
+
+    def tucker_decomposition(self, max_iters: int = 3, tol: float = 1e-4) -> list:
+        fits = (C.c_double * max_iters)()
+        it = C.c_int()
+        call("gtk_tucker_decomposition", self.handle, max_iters, tol, fits, C.byref(it))
+        return [fits[i] for i in range(it.value)]
+
+    def compute_delta(self, mode: int) -> np.ndarray:
+        d = np.empty((self.info.nnz, self.rank), self.np_dtype)
+        call("gtk_compute_delta", self.handle, mode, _ptr(d))
+        return d
+
+    # ---- timing
+    def profile(self, on: bool = True) -> None:
+        call("gtk_profile_enable", self.handle, 1 if on else 0)
+
+    def profile_read(self, kind: int) -> tuple[float, int]:
+        ms, n = C.c_double(), C.c_uint64()
+        call("gtk_profile_read", self.handle, kind, C.byref(ms), C.byref(n))
+        return ms.value, n.value
+
+    def profile_reset(self) -> None:
+        call("gtk_profile_reset", self.handle)
+
+    def timer_begin(self) -> None:
+        call("gtk_timer_begin", self.handle)
+
+    def timer_end(self) -> float:
+        ms = C.c_double()
+        call("gtk_timer_end", self.handle, C.byref(ms))
+        return ms.value
+
+    def synchronize(self) -> None:
+        call("gtk_synchronize", self.handle)
+
+    def close(self) -> None:
+        if self._h is not None:
+            nat.load().gtk_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def create_tensor_blocks(coo: Coo, partition_dims, rank: int, device: int = 0) -> BlockedTensor:
+    """CreateTensorBlocks + AssignIndicesOfEachBlock on the GPU (gtk_create_blocks)."""
+    P = np.ascontiguousarray(partition_dims, dtype=np.uint32)
+    if len(P) != coo.order:
+        raise ValueError("one partition parameter per mode")
+    h = C.c_void_p()
+    call("gtk_create_blocks", coo.handle, P.ctypes.data_as(nat.U32P), rank, device, C.byref(h))
+    return BlockedTensor(h)
+
+
+def tucker_decomposition(coo: Coo, rank: int, partition_dims=None, max_iters: int = 3, tol: float = 1e-4,
+                         rand_seed: int = 1, device: int = 0):
+    """TuckerDecomposition (tucker.cuh:30-190): blocks, init from the glibc stream that
+    continues after the parser's draws, then sweeps until max_iters or |dfit| <= tol.
+    Returns (tensor, fits)."""
+    P = partition_dims or [1] * coo.order
+    t = create_tensor_blocks(coo, P, rank, device)
+    t.init_random(rand_seed, coo.rand_draws)
+    return t, t.tucker_decomposition(max_iters, tol)

@@ -1,0 +1,194 @@
+/*
+ * gputucker_gb300.h -- C ABI of the GB300-native sparse Tucker ALS library.
+ *
+ * This is the drop-in boundary for GPUTucker's factor-update path.  Each entry
+ * point names the reference interface it replaces (paths inside the GPUTucker
+ * project).  The reference is header-only C++ templates without a C ABI; its
+ * state travels as raw pointers (Tensor<Block<uint32_t,V>>*, V*** factor slabs,
+ * double** B/C scratch).  Here that state lives behind an opaque handle in the
+ * GPU's HBM and crosses the boundary only as plain host arrays in the
+ * reference's own layouts:
+ *
+ *   coordinates ... 0-based uint32, one array per mode (Block::indices, block.hpp:171)
+ *   values ........ float or double (value_t; main.cu:25 uses double)
+ *   factor n ...... slabs concatenated: [P_n][block_dims[n]][J] row-major, the
+ *                   reference's factor_matrices[n][part][row*J+col] (tucker.cuh:71-81)
+ *   core .......... J^N values in linear order, last mode fastest (tucker.cuh:117-134)
+ *   count_nnz ..... per block and mode, block_dims[n]+1 uint64 (block.hpp:174)
+ *   where_nnz ..... per block and mode, nnz uint32 positions (block.hpp:173)
+ *
+ * Every function returns GTK_OK (0) or a GTK_ERR_* status and never exits the
+ * process or throws (the reference calls exit(1) on CUDA errors,
+ * cuda_helper.cpp:102-109, and throws std::runtime_error on bad input).
+ * gtk_last_error() returns the message of the calling thread's last failure.
+ * A handle is single-threaded: do not call into one handle from two threads at
+ * once.  All work of a handle runs on its own CUDA stream on one GPU.
+ */
+#ifndef GPUTUCKER_GB300_H_
+#define GPUTUCKER_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GTK_VERSION 1
+
+/* status codes */
+#define GTK_OK 0
+#define GTK_ERR_ARG 1         /* invalid argument (null pointer, order > 8, rank out of range ...) */
+#define GTK_ERR_IO 2          /* file cannot be opened or read */
+#define GTK_ERR_PARSE 3       /* malformed text: 0-based index, too few indices, bad number */
+#define GTK_ERR_PARTITION 4   /* infeasible P_n: ceil(dims/ceil(dims/P_n)) != P_n (tensor.tpp:199-213) */
+#define GTK_ERR_CUDA 5        /* CUDA runtime error (message in gtk_last_error) */
+#define GTK_ERR_OOM 6         /* device allocation failed or exceeds the handle's memory cap */
+#define GTK_ERR_STATE 7       /* call out of order (e.g. a sweep before the factors exist) */
+#define GTK_ERR_UNSUPPORTED 8 /* shape or option not supported by this build */
+#define GTK_ERR_NUMERIC 9     /* a row solve met a non-positive pivot (reported, factor row still written) */
+
+/* value types (the reference's value_t) */
+#define GTK_F32 0
+#define GTK_F64 1
+
+/* arithmetic forms of the sweep */
+#define GTK_PREC_PLAIN 0      /* value_t SIMT arithmetic, FP64 Gram/solve: the reference's method */
+#define GTK_PREC_BF16 1       /* delta contraction on tcgen05 tensor cores in BF16, FP32 accumulate */
+#define GTK_PREC_TF32 2       /* delta contraction on tcgen05 tensor cores in TF32, FP32 accumulate */
+
+#define GTK_MAX_ORDER 8       /* constants.hpp:16 kMaxOrder */
+#define GTK_MAX_RANK 64       /* the reference's delta kernel caps J at 50 (delta.cuh:63) */
+
+typedef struct gtk_coo gtk_coo;       /* a parsed tensor on the host (one block, global coords) */
+typedef struct gtk_tensor gtk_tensor; /* a blocked tensor + factors + core resident on one GPU */
+
+typedef struct gtk_tensor_info {
+  int order;                          /* N */
+  int rank;                           /* J */
+  int dtype;                          /* GTK_F32 / GTK_F64 */
+  int device;                         /* CUDA ordinal */
+  uint64_t nnz;
+  uint64_t block_count;               /* prod P_n */
+  uint32_t dims[GTK_MAX_ORDER];       /* max 1-based index per mode (tensor_manager.tpp:164-176) */
+  uint32_t partition_dims[GTK_MAX_ORDER];
+  uint32_t block_dims[GTK_MAX_ORDER]; /* ceil(dims/P_n) */
+  double norm;                        /* ||X||, summed in FP64 (the reference sums in value_t) */
+  uint64_t device_bytes;              /* HBM held by the handle */
+} gtk_tensor_info;
+
+/* ---- errors / version ------------------------------------------------- */
+const char *gtk_last_error(void);
+int gtk_version(void);
+
+/* ---- parsing: replaces ParseFromFile / _ReadData (tensor_manager.tpp:19-191) ----
+ * Tab- or space-separated, 1-based indices then a value, one nonzero per '\n';
+ * text after the last '\n' is ignored; dims = the largest index seen per mode.
+ * A line without a value draws frand<value_t>(0,1) from the glibc rand() stream
+ * seeded by `rand_seed` (the reference's unseeded rand() is seed 1), in file
+ * order; gtk_coo_info reports how many draws the parse consumed so that
+ * gtk_init_random can continue the same stream. */
+int gtk_parse_file(const char *path, int order, int dtype, uint32_t rand_seed, gtk_coo **out);
+int gtk_parse_buffer(const char *buf, size_t len, int order, int dtype, uint32_t rand_seed, gtk_coo **out);
+/* A COO from arrays: idx[n] -> nnz 0-based uint32 coords; values of dtype.
+ * dims may be NULL (then dims = max index + 1 per mode, as the parser does). */
+int gtk_coo_from_arrays(int order, uint64_t nnz, const uint32_t *const *idx, const void *values, int dtype,
+                        const uint32_t *dims, gtk_coo **out);
+int gtk_coo_info(const gtk_coo *coo, int *order, int *dtype, uint64_t *nnz, uint32_t *dims, uint64_t *rand_draws);
+/* copies the parsed coordinates (0-based) and values out */
+int gtk_coo_export(const gtk_coo *coo, uint32_t *const *idx, void *values);
+/* page-locks the COO's host arrays (cudaHostRegister) so gtk_create_blocks
+ * uploads them at full link speed; undone by gtk_coo_free */
+int gtk_coo_pin(gtk_coo *coo);
+void gtk_coo_free(gtk_coo *coo);
+
+/* ---- blocking: replaces CreateTensorBlocks (tensor_manager.tpp:201-302) +
+ *      Tensor::AssignIndicesOfEachBlock (tensor.tpp:139-147, block.tpp:115-186).
+ * Uploads the COO to HBM and, on the GPU, assigns block ids (last mode fastest),
+ * stable-sorts nonzeros into blocks in input order, stores block-local coords,
+ * builds the per-mode count_nnz / where_nnz of every block (bit-exact with the
+ * reference) and the per-mode row-sorted views the sweep runs on.
+ * P_n are given explicitly (the reference picks them from free GPU memory,
+ * optimizer.tpp:95-153; all-ones is its choice whenever the tensor fits).
+ * device: CUDA ordinal.  rank: J, 1..GTK_MAX_RANK. */
+int gtk_create_blocks(const gtk_coo *coo, const uint32_t *partition_dims, int rank, int device, gtk_tensor **out);
+int gtk_tensor_info_get(const gtk_tensor *t, gtk_tensor_info *info);
+/* block coordinate (N values) and nnz of one block */
+int gtk_block_info(const gtk_tensor *t, uint64_t block_id, uint32_t *coord, uint64_t *nnz);
+/* block-local coords (idx[n] -> nnz of the block) and values of one block, in the block's order */
+int gtk_block_data(const gtk_tensor *t, uint64_t block_id, uint32_t *const *idx, void *values);
+/* count_nnz (block_dims[mode]+1 uint64) and where_nnz (nnz uint32) of one block and mode */
+int gtk_block_segments(const gtk_tensor *t, uint64_t block_id, int mode, uint64_t *count_nnz, uint32_t *where_nnz);
+void gtk_destroy(gtk_tensor *t);
+
+/* ---- factors and core: replaces the init in TuckerDecomposition (tucker.cuh:71-134) ----
+ * Draws frand<double>(0,1) from the glibc rand() stream of `rand_seed` after
+ * skipping `skip_draws` draws: factor 0..N-1, slab 0..P_n-1, the real rows of the
+ * slab, column 0..J-1, then the J^N core entries in linear order.  Padding rows
+ * of the last slab are 0. */
+int gtk_init_random(gtk_tensor *t, uint32_t rand_seed, uint64_t skip_draws);
+/* slab layout [P_n * block_dims[n]][J], element type = dtype */
+int gtk_set_factor(gtk_tensor *t, int mode, const void *slabs);
+int gtk_get_factor(const gtk_tensor *t, int mode, void *slabs);
+/* J^N values, linear order */
+int gtk_set_core(gtk_tensor *t, const void *core);
+int gtk_get_core(const gtk_tensor *t, void *core);
+
+/* ---- the ALS sweep ---------------------------------------------------- */
+/* GTK_PREC_PLAIN (default), GTK_PREC_BF16 or GTK_PREC_TF32 */
+int gtk_set_precision(gtk_tensor *t, int precision);
+/* one mode update: delta, Gram/RHS (B = lambda*I + sum delta delta^T, C = sum x*delta)
+ * and the J x J row solves a = C^T B^-1, all on the GPU (update.cuh:128-199 for one mode) */
+int gtk_update_mode(gtk_tensor *t, int mode);
+/* replaces UpdateFactorMatrices (update.cuh:128-199): modes 0..N-1 in order */
+int gtk_update_factor_matrices(gtk_tensor *t);
+/* replaces Reconstruction (reconstruction.cuh:228-277): fit = 1 - sqrt(sum (x - x_hat)^2) / ||X||,
+ * with the error summed in FP64 */
+int gtk_reconstruction(gtk_tensor *t, double *fit);
+/* replaces the loop of TuckerDecomposition (tucker.cuh:166-187): up to max_iters sweeps
+ * (each UpdateFactorMatrices then Reconstruction), stopping early when
+ * |fit - previous fit| <= tol (the reference: 3 sweeps, tol = lambda = 1e-4).
+ * fits[i] receives the fit of sweep i (array of max_iters), *iters the sweeps run. */
+int gtk_tucker_decomposition(gtk_tensor *t, int max_iters, double tol, double *fits, int *iters);
+/* the delta of every nonzero for `mode` with the current factors, [nnz][J] in
+ * block-major order (the reference's per-block delta buffers concatenated,
+ * delta.cuh:206).  A parity hook: the sweep itself never writes delta to HBM. */
+int gtk_compute_delta(gtk_tensor *t, int mode, void *delta);
+
+/* ---- data on either side of the path ----------------------------------
+ * No reference counterpart: the reference only reads files it did not make.
+ * gtk_generate draws `nnz` distinct coordinates (each mode uniform, or
+ * Zipf(zipf_s) over a seeded permutation of the axis) and values (uniform
+ * [0,1), or lognormal(0,1) scaled by its maximum to [0,1]); dims of the result
+ * are the largest index drawn + 1, as the parser would report.  Deterministic
+ * in `seed` whatever the host thread count.  gtk_generate_planted draws uniform
+ * coordinates and values of a planted Tucker model (core and nonnegative
+ * factors uniform [0,1) of rank planted_rank) plus N(0, noise_sigma^2).
+ * gtk_write_text writes the reference's text format (1-based, tab-separated). */
+#define GTK_GEN_UNIFORM 0
+#define GTK_GEN_ZIPF 1
+#define GTK_VAL_UNIFORM 0
+#define GTK_VAL_LOGNORMAL 1
+#define GTK_VAL_PLANTED 2
+int gtk_generate(int order, const uint32_t *dims, uint64_t nnz, int index_dist, double zipf_s, int value_dist,
+                 int dtype, uint64_t seed, gtk_coo **out);
+int gtk_generate_planted(int order, const uint32_t *dims, uint64_t nnz, int planted_rank, double noise_sigma,
+                         int dtype, uint64_t seed, gtk_coo **out);
+int gtk_write_text(const gtk_coo *coo, const char *path);
+
+/* ---- timing ----------------------------------------------------------- */
+/* Per-kernel device time accumulated with CUDA events on the handle's stream
+ * while enabled.  kind: 0 delta+gram, 1 solve, 2 fit, 3 all sweep kernels. */
+int gtk_profile_enable(gtk_tensor *t, int on);
+int gtk_profile_read(gtk_tensor *t, int kind, double *ms, uint64_t *launches);
+int gtk_profile_reset(gtk_tensor *t);
+/* events on the handle's stream: begin records, end records + waits and returns ms */
+int gtk_timer_begin(gtk_tensor *t);
+int gtk_timer_end(gtk_tensor *t, double *ms);
+int gtk_synchronize(gtk_tensor *t);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUTUCKER_GB300_H_ */

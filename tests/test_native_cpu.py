@@ -1,0 +1,198 @@
+"""The native library on the CPU: exports, host-side parsing/generation, argument errors.
+
+No kernel runs here; everything below is host code of libgputucker_gb300.so
+(the GPU paths are in the tests marked gpu).
+"""
+
+import ctypes as C
+import glob
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import gputucker_gb300 as gtk
+from gputucker_gb300 import _native as nat
+from oracle_util import ROOT, ora_parse
+
+HEADER = os.path.join(ROOT, "include", "gputucker_gb300.h")
+GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
+
+
+def header_functions():
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(gtk_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_function(native):
+    names = header_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(native, n)]
+    assert not missing, missing
+    # and the Python binding declares a signature for each
+    assert set(names) <= set(nat.SIGNATURES), set(names) - set(nat.SIGNATURES)
+
+
+def test_version(native):
+    assert native.gtk_version() == 1
+
+
+PARSE_TEXTS = [
+    b"1\t2\t3\t0.5\n2 3 4 0.25\n",
+    b"1\t2\t3\t0.5\n4\t4\t4\t1.5\ntrailing text without newline",
+    b"1\t1\t1\n2\t2\t2\t0.75\n3\t3\t3\n5\t1\t2\n",
+    b"1\t2\t3\t0.5\r\n2\t3\t4\t0.25\r\n",
+    b"  1 \t 2\t3   7e-1\n",
+    b"7\t8\t9\t1e-3 extra tokens ignored\n",
+    b"",
+    b"no newline at all",
+]
+
+
+@pytest.mark.parametrize("text", PARSE_TEXTS)
+@pytest.mark.parametrize("dtype", [0, 1])
+def test_parser_matches_oracle(native, text, dtype):
+    rc, idx, vals, dims, draws = ora_parse(text, 3, dtype, seed=1)
+    assert rc == 0
+    coo = gtk.parse_buffer(text, 3, dtype, rand_seed=1)
+    gi, gv = coo.arrays()
+    assert coo.nnz == len(vals)
+    if coo.nnz:
+        assert coo.dims == dims
+    assert coo.rand_draws == draws
+    for n in range(3):
+        np.testing.assert_array_equal(gi[n], idx[n])
+    np.testing.assert_array_equal(gv, vals)
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_parser_matches_reference_golden(native, path):
+    g = np.load(path)
+    N = len(g["dims"])
+    coo = gtk.parse_from_file(path[:-4] + ".tns", N, int(g["dtype"]), rand_seed=1)
+    idx, vals = coo.arrays()
+    assert coo.dims == [int(x) for x in g["dims"]]
+    assert coo.rand_draws == int(g["skip"])
+    for n in range(N):
+        np.testing.assert_array_equal(idx[n], g[f"parsed_idx{n}"])
+    np.testing.assert_array_equal(vals, g["parsed_vals"])
+
+
+@pytest.mark.parametrize("text,code", [
+    (b"1\t0\t3\t0.5\n", nat.GTK_ERR_PARSE),         # 0 is not a 1-based index
+    (b"1\t2\n", nat.GTK_ERR_PARSE),                 # fewer indices than the order
+    (b"1\t2\t3\t0.5\n\n", nat.GTK_ERR_PARSE),       # empty line
+    (b"1\t2\t3\tabc\n", nat.GTK_ERR_PARSE),         # value that is not a number
+    (b"# comment\n1\t2\t3\t0.5\n", nat.GTK_ERR_PARSE),  # the format has no comments
+])
+def test_parser_errors(native, text, code):
+    with pytest.raises(gtk.GTKError) as e:
+        gtk.parse_buffer(text, 3, "f64")
+    assert e.value.code == code
+
+
+def test_parse_missing_file(native):
+    with pytest.raises(gtk.GTKError) as e:
+        gtk.parse_from_file("/nonexistent/x.tns", 3)
+    assert e.value.code == nat.GTK_ERR_IO
+
+
+@pytest.mark.parametrize("order", [0, 9])
+def test_parse_bad_order(native, order):
+    with pytest.raises(gtk.GTKError) as e:
+        gtk.parse_buffer(b"1 1 1 1\n", order)
+    assert e.value.code == nat.GTK_ERR_ARG
+
+
+def test_parser_large_multithreaded_matches_oracle(native, tmp_path):
+    coo = gtk.generate(3, [5000, 6000, 7000], 300_000, "zipf", 1.2, "uniform", "f64", seed=3)
+    p = tmp_path / "big.tns"
+    coo.write_text(str(p))
+    data = p.read_bytes()
+    rc, idx, vals, dims, _ = ora_parse(data, 3, 1)
+    assert rc == 0
+    back = gtk.parse_from_file(str(p), 3, "f64")
+    bi, bv = back.arrays()
+    gi, gv = coo.arrays()
+    for n in range(3):
+        np.testing.assert_array_equal(bi[n], idx[n])
+        np.testing.assert_array_equal(bi[n], gi[n])
+    np.testing.assert_array_equal(bv, vals)
+    np.testing.assert_array_equal(bv, gv)  # %.17g round-trips doubles
+    assert back.dims == dims == coo.dims
+
+
+def test_f32_text_roundtrip(native, tmp_path):
+    coo = gtk.generate(4, [300] * 4, 20_000, "uniform", 0, "uniform", "f32", seed=1)
+    p = tmp_path / "f.tns"
+    coo.write_text(str(p))
+    back = gtk.parse_from_file(str(p), 4, "f32")
+    np.testing.assert_array_equal(back.arrays()[1], coo.arrays()[1])
+
+
+def test_generator_deterministic_and_distinct(native):
+    a = gtk.generate(4, [1000] * 4, 50_000, "zipf", 1.1, "uniform", "f32", seed=5)
+    b = gtk.generate(4, [1000] * 4, 50_000, "zipf", 1.1, "uniform", "f32", seed=5)
+    c = gtk.generate(4, [1000] * 4, 50_000, "zipf", 1.1, "uniform", "f32", seed=6)
+    ai, av = a.arrays()
+    bi, bv = b.arrays()
+    ci, _ = c.arrays()
+    for n in range(4):
+        np.testing.assert_array_equal(ai[n], bi[n])
+    np.testing.assert_array_equal(av, bv)
+    assert any((ai[n] != ci[n]).any() for n in range(4))
+    keys = np.stack(ai, 1)
+    assert len(np.unique(keys, axis=0)) == len(keys)
+    # power-law slices: the heaviest slice holds far more than the mean
+    counts = np.bincount(ai[0])
+    assert counts.max() > 20 * counts.mean()
+    assert av.min() >= 0 and av.max() < 1
+
+
+def test_generator_lognormal_scaled(native):
+    a = gtk.generate(3, [2000] * 3, 20_000, "zipf", 1.05, "lognormal", "f32", seed=2)
+    v = a.arrays()[1]
+    assert v.max() == pytest.approx(1.0) and v.min() > 0
+
+
+def test_generator_planted(native):
+    a = gtk.generate_planted(3, [200] * 3, 5000, 4, 0.01, "f32", seed=1)
+    v = a.arrays()[1]
+    assert a.nnz == 5000 and v.mean() > 1.0  # sum of 64 positive products
+
+
+@pytest.mark.parametrize("P,code", [([6, 1, 1], nat.GTK_ERR_PARTITION), ([0, 1, 1], nat.GTK_ERR_ARG)])
+def test_create_blocks_rejects_bad_partition(native, P, code):
+    coo = gtk.coo_from_arrays([np.array([0, 9], np.uint32)] * 3, np.array([1.0, 2.0]), dims=[10, 10, 10])
+    with pytest.raises(gtk.GTKError) as e:
+        gtk.create_tensor_blocks(coo, P, 4)
+    assert e.value.code == code
+
+
+@pytest.mark.parametrize("rank", [0, 65])
+def test_create_blocks_rejects_rank(native, rank):
+    coo = gtk.coo_from_arrays([np.array([0, 1], np.uint32)] * 3, np.array([1.0, 2.0]))
+    with pytest.raises(gtk.GTKError) as e:
+        gtk.create_tensor_blocks(coo, [1, 1, 1], rank)
+    assert e.value.code == nat.GTK_ERR_ARG
+
+
+def test_coo_from_arrays_bounds(native):
+    with pytest.raises(gtk.GTKError) as e:
+        gtk.coo_from_arrays([np.array([0, 10], np.uint32)] * 2, np.array([1.0, 2.0]), dims=[10, 10])
+    assert e.value.code == nat.GTK_ERR_ARG
+
+
+def test_cli_usage(native):
+    from gputucker_gb300 import build
+    cli = build.CLI
+    assert os.path.exists(cli)
+    r = subprocess.run([cli, "-h"], capture_output=True, text=True)
+    assert r.returncode == 0 and "--input" in r.stdout
+    r = subprocess.run([cli, "-o", "3"], capture_output=True, text=True)
+    assert r.returncode == 2 and "Input file must be specified" in r.stdout
+    r = subprocess.run([cli, "-i", "/nonexistent", "-o", "3"], capture_output=True, text=True)
+    assert r.returncode == 2
