@@ -62,7 +62,9 @@ def args_parse():
     p.add_argument("--e2e-runs", type=int, default=1)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
-    p.add_argument("--cpu-sample", type=int, default=1_000_000, help="nonzeros in the CPU baseline sample")
+    p.add_argument("--cpu-sample", type=int, default=500_000, help="nonzeros in the CPU baseline sample")
+    p.add_argument("--ref-sample", type=int, default=200_000, help="nonzeros per reference-arm step")
+    p.add_argument("--precision", choices=["plain", "bf16", "tf32"], default="plain")
     return p.parse_args()
 
 
@@ -181,24 +183,24 @@ def run_reference(args, cfg, dist):
     if dist.rank != 0:
         return
     nnz = args.nnz or cfg["nnz"]
-    coo, _ = gen_workload(cfg, min(nnz, args.cpu_sample * 4))
+    coo, _ = gen_workload(cfg, min(nnz, args.ref_sample * 4))
     steps = max(1, args.steps)
     import numpy as np  # noqa: F401
     res = None
     vals = []
     for _ in range(args.warmup and 1):
-        cpu_baseline(coo, cfg, args.cpu_sample, 1)
+        cpu_baseline(coo, cfg, args.ref_sample, 1)
     for _ in range(steps):
-        res = cpu_baseline(coo, cfg, args.cpu_sample, 1)
+        res = cpu_baseline(coo, cfg, args.ref_sample, 1)
         vals.append(res["value"])
     v = statistics.median(vals)
     res["value"] = v
     line = {
         "impl": "reference", "metric": "ALS-sweep nnz/s (plain FP32, 1 device)", "value": v, "unit": "nnz/s",
-        "n_gpus": dist.world, "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * cfg["order"] * args.cpu_sample / v,
+        "n_gpus": dist.world, "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * cfg["order"] * args.ref_sample / v,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {k: cfg[k] for k in ("workload", "order", "dims", "zipf_s", "rank", "partition", "dtype")}
-        | {"nnz": nnz, "sample_nnz": min(args.cpu_sample, coo.nnz)},
+        | {"nnz": nnz, "sample_nnz": min(args.ref_sample, coo.nnz)},
         "cpu_baseline": res,
         "e2e": {"value": v, "unit": "nnz/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
@@ -224,6 +226,7 @@ def main():
     # ---- device-resident sweeps
     t = gtk.create_tensor_blocks(coo, cfg["partition"], J, device=device)
     t.init_random(1, 0)
+    t.set_precision(args.precision)
     for _ in range(max(3, args.warmup)):
         t.update_factor_matrices()
         t.reconstruction()
@@ -246,7 +249,7 @@ def main():
     s_ms, s_n = t.profile_read(1)
     f_ms, f_n = t.profile_read(2)
     t.profile(False)
-    launches = int(k_n + s_n + 2 * f_n)  # fused + solve per mode, fit + its final sum per sweep
+    launches = int(k_n + s_n + f_n)  # fused + solve per mode; the fit is one final sum (its error comes from the last solve)
     ms_step = ms / args.steps
     value = dist.world * N * nnz * args.steps / (ms / 1e3)
     # ---- roofline of the dominant kernel (fused delta + Gram/RHS)
@@ -289,6 +292,7 @@ def main():
             t0 = time.perf_counter()
             tt = gtk.create_tensor_blocks(coo, cfg["partition"], J, device=device)
             tt.init_random(1, 0)
+            tt.set_precision(args.precision)
             for _ in range(sweeps):
                 tt.update_factor_matrices()
                 tt.reconstruction()
@@ -309,7 +313,7 @@ def main():
         cpu = cpu_baseline(coo, cfg, args.cpu_sample)
     if dist.rank == 0:
         line = {
-            "metric": "ALS-sweep nnz/s (plain FP32, 1 GB300)", "value": value, "unit": "nnz/s", "n_gpus": dist.world,
+            "metric": f"ALS-sweep nnz/s ({args.precision}, FP32 values, 1 GB300)", "value": value, "unit": "nnz/s", "n_gpus": dist.world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {k: cfg[k] for k in ("workload", "order", "dims", "zipf_s", "rank", "partition", "dtype")}

@@ -20,7 +20,7 @@ int parse_file(const char *path, int N, int dtype, uint32_t seed, gtk_coo *out);
 
 namespace {
 thread_local std::string g_err;
-constexpr int kPartialDoubles = 2048;
+constexpr int kPartialDoubles = 2048;  // per-CTA partial sums (fit, norm) + their total
 
 uint64_t memory_cap() {
   const char *s = getenv("GTK_DEVICE_MEMORY_CAP");
@@ -70,6 +70,7 @@ static void release(DevTensor &t) {
 
 // slab layout [rows][J] <-> device [rows][ldf]
 static int put_factor(DevTensor &t, int n, const void *slabs) {
+  t.fit_from_gram = false;
   GTK_CUDA(cudaMemcpy2DAsync(t.fac[n], (size_t)t.ldf * t.vsize, slabs, (size_t)t.J * t.vsize, (size_t)t.J * t.vsize,
                              t.rows[n], cudaMemcpyHostToDevice, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
@@ -84,6 +85,7 @@ static int get_factor(const DevTensor &t, int n, void *slabs) {
 }
 
 static int put_core(DevTensor &t, const void *core) {
+  t.fit_from_gram = false;
   GTK_CUDA(cudaMemcpyAsync(t.core, core, t.core_n * t.vsize, cudaMemcpyHostToDevice, t.stream));
   if (int rc = upload_core_perms(t, core)) return rc;
   t.have_core = true;
@@ -94,10 +96,10 @@ static int check_status(DevTensor &t) {
   int st = 0;
   GTK_CUDA(cudaMemcpyAsync(&st, t.status, 4, cudaMemcpyDeviceToHost, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
-  if (st) {
-    GTK_CUDA(cudaMemsetAsync(t.status, 0, 4, t.stream));
-    return fail(GTK_ERR_NUMERIC, "a row solve met a non-positive pivot");
-  }
+  if (st & 4) t.lu_fallbacks += 1;  // Cholesky gave way to pivoted LU somewhere: informational
+  if (st) GTK_CUDA(cudaMemsetAsync(t.status, 0, 4, t.stream));
+  if (st & 2) return fail(GTK_ERR_CUDA, "a tensor-core kernel gave up waiting for its MMAs");
+  if (st & 1) return fail(GTK_ERR_NUMERIC, "a row system was singular (zero LU pivot)");
   return 0;
 }
 
@@ -261,7 +263,7 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
   t->J = rank;
   const int w = (int)(16 / t->vsize);
   t->ldf = (rank + w - 1) / w * w;
-  t->E = (rank + 1) * (rank + 2) / 2 - 1;
+  t->E = (rank + 1) * (rank + 2) / 2;
   t->nnz = coo->nnz;
   t->nblk = nblk;
   t->core_n = core_n;
@@ -460,7 +462,12 @@ int gtk_get_core(const gtk_tensor *t, void *core) {
 
 int gtk_set_precision(gtk_tensor *t, int precision) {
   if (!t) return fail(GTK_ERR_ARG, "null tensor");
-  if (precision != GTK_PREC_PLAIN) return fail(GTK_ERR_UNSUPPORTED, "only GTK_PREC_PLAIN is built");
+  if (precision != GTK_PREC_PLAIN && precision != GTK_PREC_BF16 && precision != GTK_PREC_TF32)
+    return fail(GTK_ERR_ARG, "unknown precision");
+  t->fit_from_gram = false;
+  if (precision != GTK_PREC_PLAIN && !tc_supported(t->N, t->J, t->dtype))
+    return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this order/rank/value type (FP32, N = 3 or 4, "
+                                     "J in {4, 8, 10, 12, 16} for N = 3 and {4, 8, 10, 12} for N = 4)");
   t->precision = precision;
   return 0;
 }

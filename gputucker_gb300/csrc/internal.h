@@ -122,6 +122,9 @@ struct DevTensor {
   double *partial = nullptr;  // fit partial sums
   int *status = nullptr;      // device status words (numeric flags)
   int num_sms = 0;
+  uint64_t lu_fallbacks = 0;
+  bool fit_from_gram = false;  // partials hold the fit error of the last mode's update
+  int fit_grid = 0;  // sweeps in which some row needed the pivoted-LU fallback
 
   // profiling
   bool prof = false;
@@ -144,6 +147,9 @@ int upload_core_perms(DevTensor &t, const void *core_host);
 int run_update_mode(DevTensor &t, int mode);
 int run_fit(DevTensor &t, double *fit);
 int run_delta(DevTensor &t, int mode, void *d_delta_blockmajor);
+// tc_sweep.cu: the tensor-core (BF16 / TF32) form; kind 0 update, 1 fit, 2 delta
+bool tc_supported(int N, int J, int dtype);
+int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used);
 // per-kernel CUDA-event timing on the handle's stream (kind 0 delta+gram, 1 solve, 2 fit)
 int prof_begin(DevTensor &t, cudaEvent_t *a);
 int prof_end(DevTensor &t, int kind, cudaEvent_t a);

@@ -1,0 +1,220 @@
+// mode_common.cuh -- device pieces shared by the mode kernels (SIMT and tcgen05):
+// the kernel argument block, the shared tile layout and the row-segmented
+// Gram/RHS reduction of a tile of delta rows.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "internal.h"
+
+namespace gtk {
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kFitGridMax = 1024;
+
+enum Kind { kUpdate = 0, kFit = 1, kDelta = 2 };
+
+template <int B, int E> struct Pow { static constexpr int v = B * Pow<B, E - 1>::v; };
+template <int B> struct Pow<B, 0> { static constexpr int v = 1; };
+
+struct ModeArgs {
+  const uint32_t *coord[kMaxOrder];  // view coordinates (global), coord[mode] = row
+  const void *val;                   // view values
+  const void *fac[kMaxOrder];        // factor matrices, row stride ldf
+  const void *corep;                 // [J^(N-1)][ldf], mode first
+  const uint32_t *vperm;             // view -> block-major position (kDelta)
+  void *out;                         // kDelta: delta [nnz][J] block-major
+  double *gram;                      // kUpdate: [rows][E]
+  double *partial;                   // kFit: per-CTA error sums
+  int *status;                       // device status word (bit 1: a bounded wait gave up)
+  uint64_t nnz;
+  int N, J, ldf, mode, E, ldd;
+  int others[kMaxOrder];             // the other modes in increasing order
+  uint64_t gp_elems;                 // J^(N-1) * ldf
+  int gp_in_smem;                    // generic kernel: core in shared memory?
+};
+
+// ---------------------------------------------------------------- vector loads
+template <class V> struct Vec;
+template <> struct Vec<float> {
+  using T = float4;
+  static constexpr int W = 4;
+  __device__ static void unpack(const T &v, float *o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
+};
+template <> struct Vec<double> {
+  using T = double2;
+  static constexpr int W = 2;
+  __device__ static void unpack(const T &v, double *o) { o[0] = v.x; o[1] = v.y; }
+};
+
+// ---------------------------------------------------------------- shared tile layout
+template <class V> struct TileSmem {
+  // carve: [gp][arow][dx][rows][seg_start][pairs]
+  V *gp;
+  V *arow;
+  V *dx;
+  uint32_t *rows;
+  uint32_t *seg;
+  unsigned char *pi, *pj;
+};
+
+__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Shared memory needed by a tile of `tn` nonzeros.
+inline size_t tile_smem_bytes(size_t vsize, size_t gp_elems, int arow_levels, int npt, int J, int ldd, int E,
+                              int tn) {
+  size_t b = align_up(gp_elems * vsize, 16);
+  b += align_up((size_t)arow_levels * npt * J * kThreads * vsize, 16);
+  b += align_up((size_t)tn * ldd * vsize, 16);
+  b += align_up((size_t)tn * 4, 16);
+  b += align_up((size_t)(tn + 1) * 4, 16);
+  b += align_up((size_t)E * 2, 16);
+  return b;
+}
+
+template <class V>
+__device__ TileSmem<V> carve(unsigned char *base, size_t gp_elems, int arow_levels, int npt, int J, int ldd, int E,
+                             int tn) {
+  TileSmem<V> s;
+  size_t off = 0;
+  s.gp = reinterpret_cast<V *>(base + off);
+  off += align_up(gp_elems * sizeof(V), 16);
+  s.arow = reinterpret_cast<V *>(base + off);
+  off += align_up((size_t)arow_levels * npt * J * kThreads * sizeof(V), 16);
+  s.dx = reinterpret_cast<V *>(base + off);
+  off += align_up((size_t)tn * ldd * sizeof(V), 16);
+  s.rows = reinterpret_cast<uint32_t *>(base + off);
+  off += align_up((size_t)tn * 4, 16);
+  s.seg = reinterpret_cast<uint32_t *>(base + off);
+  off += align_up((size_t)(tn + 1) * 4, 16);
+  s.pi = base + off;
+  s.pj = base + off + E;
+  return s;
+}
+
+// pair table of the Gram/RHS entries: e -> (i, j), 0 <= i <= j <= J, row-major
+// over the upper triangle.  Column J of the delta tile holds x, so (i, J) is the
+// right-hand side C_i = sum x*delta_i and the last entry (J, J) is sum x^2 of the
+// row, which the fit uses (sum (x - delta.a)^2 = sum x^2 - 2 a.C + a^T G a).
+__device__ void fill_pairs(unsigned char *pi, unsigned char *pj, int J) {
+  if (threadIdx.x == 0) {
+    int e = 0;
+    for (int i = 0; i <= J; ++i)
+      for (int j = i; j <= J; ++j) {
+        pi[e] = (unsigned char)i;
+        pj[e] = (unsigned char)j;
+        ++e;
+      }
+  }
+}
+
+// an un-contractible product (never fused into an FMA with the following add)
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+
+template <class V> struct ProdSum {
+  double s = 0;
+  __device__ void add(V p) { s += (double)p; }
+  __device__ double value() const { return s; }
+};
+template <> struct ProdSum<float> {
+  float s = 0.f, c = 0.f;
+  __device__ void add(float p) {
+    const float t = s + p;
+    c += (fabsf(s) >= fabsf(p)) ? ((s - t) + p) : ((p - t) + s);
+    s = t;
+  }
+  __device__ double value() const { return (double)s + (double)c; }
+};
+
+// Row-segmented reduction of the tile into the FP64 Gram/RHS rows.
+// tile_start: view position of tile element 0; nv: valid elements in the tile.
+template <class V>
+__device__ void gram_phase(const ModeArgs &a, const TileSmem<V> &s, uint64_t tile_start, int nv, int npt) {
+  const int tid = threadIdx.x;
+  __shared__ uint32_t sw[32];
+  __shared__ uint32_t nseg_s;
+  // segment heads over contiguous chunks of npt positions per thread
+  uint32_t cnt = 0;
+  for (int k = 0; k < npt; ++k) {
+    int t = tid * npt + k;
+    if (t < nv && (t == 0 || s.rows[t] != s.rows[t - 1])) ++cnt;
+  }
+  // block exclusive scan of cnt
+  {
+    const int lane = tid & 31, warp = tid >> 5;
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) sw[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+      const int nw = (int)(blockDim.x >> 5);
+      uint32_t w = lane < nw ? sw[lane] : 0u;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
+        if (lane >= o) w += y;
+      }
+      if (lane < nw) sw[lane] = w;
+      if (lane == nw - 1) nseg_s = w;
+    }
+    __syncthreads();
+    uint32_t id = (warp > 0 ? sw[warp - 1] : 0u) + x - cnt;
+    for (int k = 0; k < npt; ++k) {
+      int t = tid * npt + k;
+      if (t < nv && (t == 0 || s.rows[t] != s.rows[t - 1])) s.seg[id++] = (uint32_t)t;
+    }
+    if (tid == 0) s.seg[nseg_s] = (uint32_t)nv;
+  }
+  __syncthreads();
+  const int nseg = (int)nseg_s;
+  const int E = a.E, ldd = a.ldd;
+  // does the tile hold the whole first / last row?
+  const uint32_t first_row = s.rows[0], last_row = nv > 0 ? s.rows[nv - 1] : 0u;
+  const bool first_open = tile_start > 0 && a.coord[a.mode][tile_start - 1] == first_row;
+  const bool last_open = tile_start + nv < a.nnz && a.coord[a.mode][tile_start + nv] == last_row;
+  const int items = nseg * E;
+  for (int w = tid; w < items; w += (int)blockDim.x) {
+    const int sgi = w / E, e = w - sgi * E;
+    const int i = s.pi[e], j = s.pj[e];
+    const int t0 = (int)s.seg[sgi], t1 = (int)s.seg[sgi + 1];
+    ProdSum<V> acc;
+    for (int t = t0; t < t1; ++t) acc.add(mul_rn(s.dx[t * ldd + i], s.dx[t * ldd + j]));
+    const uint32_t row = s.rows[t0];
+    double *dst = a.gram + (size_t)row * E + e;
+    const bool shared_row = (sgi == 0 && first_open) || (sgi == nseg - 1 && last_open);
+    if (shared_row)
+      atomicAdd(dst, acc.value());
+    else
+      *dst = acc.value();
+  }
+}
+
+
+__device__ inline double block_sum(double v) {
+  __shared__ double sw[32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
+  if (lane == 0) sw[warp] = v;
+  __syncthreads();
+  double s = 0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sw[w];
+  __syncthreads();
+  return s;  // valid in thread 0
+}
+
+
+inline int ldd_for(int J) { return ((J + 1) & 1) ? J + 1 : J + 2; }
+inline int pairs_for(int J) { return (J + 1) * (J + 2) / 2; }
+
+}  // namespace
+}  // namespace gtk

@@ -36,46 +36,10 @@
 #include <vector>
 
 #include "internal.h"
+#include "mode_common.cuh"
 
 namespace gtk {
 namespace {
-
-constexpr int kThreads = 256;
-constexpr int kFitGridMax = 1024;
-
-enum Kind { kUpdate = 0, kFit = 1, kDelta = 2 };
-
-template <int B, int E> struct Pow { static constexpr int v = B * Pow<B, E - 1>::v; };
-template <int B> struct Pow<B, 0> { static constexpr int v = 1; };
-
-struct ModeArgs {
-  const uint32_t *coord[kMaxOrder];  // view coordinates (global), coord[mode] = row
-  const void *val;                   // view values
-  const void *fac[kMaxOrder];        // factor matrices, row stride ldf
-  const void *corep;                 // [J^(N-1)][ldf], mode first
-  const uint32_t *vperm;             // view -> block-major position (kDelta)
-  void *out;                         // kDelta: delta [nnz][J] block-major
-  double *gram;                      // kUpdate: [rows][E]
-  double *partial;                   // kFit: per-CTA error sums
-  uint64_t nnz;
-  int N, J, ldf, mode, E, ldd;
-  int others[kMaxOrder];             // the other modes in increasing order
-  uint64_t gp_elems;                 // J^(N-1) * ldf
-  int gp_in_smem;                    // generic kernel: core in shared memory?
-};
-
-// ---------------------------------------------------------------- vector loads
-template <class V> struct Vec;
-template <> struct Vec<float> {
-  using T = float4;
-  static constexpr int W = 4;
-  __device__ static void unpack(const T &v, float *o) { o[0] = v.x; o[1] = v.y; o[2] = v.z; o[3] = v.w; }
-};
-template <> struct Vec<double> {
-  using T = double2;
-  static constexpr int W = 2;
-  __device__ static void unpack(const T &v, double *o) { o[0] = v.x; o[1] = v.y; }
-};
 
 // ---------------------------------------------------------------- contraction nest
 // Nest<D> contracts D other modes.  g: the core sub-block for the current outer
@@ -129,149 +93,6 @@ template <class V, int J, int LDG, int NPT> struct Nest<V, J, LDG, NPT, 2> {
   }
 };
 
-// ---------------------------------------------------------------- shared tile layout
-template <class V> struct TileSmem {
-  // carve: [gp][arow][dx][rows][seg_start][pairs]
-  V *gp;
-  V *arow;
-  V *dx;
-  uint32_t *rows;
-  uint32_t *seg;
-  unsigned char *pi, *pj;
-};
-
-__host__ __device__ inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
-
-// Shared memory needed by a tile of `tn` nonzeros.
-inline size_t tile_smem_bytes(size_t vsize, size_t gp_elems, int arow_levels, int npt, int J, int ldd, int E,
-                              int tn) {
-  size_t b = align_up(gp_elems * vsize, 16);
-  b += align_up((size_t)arow_levels * npt * J * kThreads * vsize, 16);
-  b += align_up((size_t)tn * ldd * vsize, 16);
-  b += align_up((size_t)tn * 4, 16);
-  b += align_up((size_t)(tn + 1) * 4, 16);
-  b += align_up((size_t)E * 2, 16);
-  return b;
-}
-
-template <class V>
-__device__ TileSmem<V> carve(unsigned char *base, size_t gp_elems, int arow_levels, int npt, int J, int ldd, int E,
-                             int tn) {
-  TileSmem<V> s;
-  size_t off = 0;
-  s.gp = reinterpret_cast<V *>(base + off);
-  off += align_up(gp_elems * sizeof(V), 16);
-  s.arow = reinterpret_cast<V *>(base + off);
-  off += align_up((size_t)arow_levels * npt * J * kThreads * sizeof(V), 16);
-  s.dx = reinterpret_cast<V *>(base + off);
-  off += align_up((size_t)tn * ldd * sizeof(V), 16);
-  s.rows = reinterpret_cast<uint32_t *>(base + off);
-  off += align_up((size_t)tn * 4, 16);
-  s.seg = reinterpret_cast<uint32_t *>(base + off);
-  off += align_up((size_t)(tn + 1) * 4, 16);
-  s.pi = base + off;
-  s.pj = base + off + E;
-  return s;
-}
-
-// pair table of the Gram/RHS entries: e -> (i, j), i <= j <= J, except (J, J).
-// Column J of the delta tile holds x, so (i, J) is the right-hand side C_i.
-__device__ void fill_pairs(unsigned char *pi, unsigned char *pj, int J) {
-  if (threadIdx.x == 0) {
-    int e = 0;
-    for (int i = 0; i <= J; ++i)
-      for (int j = i; j <= J; ++j) {
-        if (i == J && j == J) continue;
-        pi[e] = (unsigned char)i;
-        pj[e] = (unsigned char)j;
-        ++e;
-      }
-  }
-}
-
-template <class V> struct Acc { using T = V; };
-
-// Row-segmented reduction of the tile into the FP64 Gram/RHS rows.
-// tile_start: view position of tile element 0; nv: valid elements in the tile.
-template <class V>
-__device__ void gram_phase(const ModeArgs &a, const TileSmem<V> &s, uint64_t tile_start, int nv, int npt) {
-  using A = typename Acc<V>::T;
-  const int tid = threadIdx.x;
-  __shared__ uint32_t sw[32];
-  __shared__ uint32_t nseg_s;
-  // segment heads over contiguous chunks of npt positions per thread
-  uint32_t cnt = 0;
-  for (int k = 0; k < npt; ++k) {
-    int t = tid * npt + k;
-    if (t < nv && (t == 0 || s.rows[t] != s.rows[t - 1])) ++cnt;
-  }
-  // block exclusive scan of cnt
-  {
-    const int lane = tid & 31, warp = tid >> 5;
-    uint32_t x = cnt;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
-      if (lane >= o) x += y;
-    }
-    if (lane == 31) sw[warp] = x;
-    __syncthreads();
-    if (warp == 0) {
-      uint32_t w = lane < (kThreads / 32) ? sw[lane] : 0u;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xFFFFFFFFu, w, o);
-        if (lane >= o) w += y;
-      }
-      if (lane < kThreads / 32) sw[lane] = w;
-      if (lane == kThreads / 32 - 1) nseg_s = w;
-    }
-    __syncthreads();
-    uint32_t id = (warp > 0 ? sw[warp - 1] : 0u) + x - cnt;
-    for (int k = 0; k < npt; ++k) {
-      int t = tid * npt + k;
-      if (t < nv && (t == 0 || s.rows[t] != s.rows[t - 1])) s.seg[id++] = (uint32_t)t;
-    }
-    if (tid == 0) s.seg[nseg_s] = (uint32_t)nv;
-  }
-  __syncthreads();
-  const int nseg = (int)nseg_s;
-  const int E = a.E, ldd = a.ldd;
-  // does the tile hold the whole first / last row?
-  const uint32_t first_row = s.rows[0], last_row = nv > 0 ? s.rows[nv - 1] : 0u;
-  const bool first_open = tile_start > 0 && a.coord[a.mode][tile_start - 1] == first_row;
-  const bool last_open = tile_start + nv < a.nnz && a.coord[a.mode][tile_start + nv] == last_row;
-  const int items = nseg * E;
-  for (int w = tid; w < items; w += kThreads) {
-    const int sgi = w / E, e = w - sgi * E;
-    const int i = s.pi[e], j = s.pj[e];
-    const int t0 = (int)s.seg[sgi], t1 = (int)s.seg[sgi + 1];
-    A acc = A(0);
-    for (int t = t0; t < t1; ++t) acc += (A)s.dx[t * ldd + i] * (A)s.dx[t * ldd + j];
-    const uint32_t row = s.rows[t0];
-    double *dst = a.gram + (size_t)row * E + e;
-    const bool shared_row = (sgi == 0 && first_open) || (sgi == nseg - 1 && last_open);
-    if (shared_row)
-      atomicAdd(dst, (double)acc);
-    else
-      *dst = (double)acc;
-  }
-}
-
-
-__device__ inline double block_sum(double v) {
-  __shared__ double sw[32];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xFFFFFFFFu, v, o);
-  if (lane == 0) sw[warp] = v;
-  __syncthreads();
-  double s = 0;
-  if (threadIdx.x == 0)
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sw[w];
-  __syncthreads();
-  return s;  // valid in thread 0
-}
 
 // ---------------------------------------------------------------- specialised kernel
 // Compile-time order N and rank J; NPT nonzeros per thread share every core read.
@@ -459,72 +280,190 @@ __global__ void __launch_bounds__(kThreads) k_mode_gen(ModeArgs a) {
 }
 
 // ---------------------------------------------------------------- row solves
-// One warp per factor row: A = lambda I + Gram (FP64), Cholesky A = L L^T in
-// shared memory, L y = C, L^T a = y; a (cast to value_t) overwrites the row.
-// A non-positive pivot sets bit 0 of *status (the reference's Eigen inverse
-// would return inf/nan there); the row is still written.
+// One warp per factor row: A = lambda I + Gram (FP64) in shared memory.
+// First Cholesky A = L L^T, L y = C, L^T a = y (A is symmetric positive definite
+// in exact arithmetic).  When rounding makes a pivot non-positive -- rows with
+// fewer nonzeros than J after ill-conditioned updates -- the row is solved again
+// by LU with partial pivoting, the method of the reference's Eigen inverse
+// (update.cuh:180), and bit 2 of *status counts it as a fallback (informational).
+// An exactly zero LU pivot sets bit 0 (GTK_ERR_NUMERIC); the row is still written.
+// decode entry e of the packed row into (i, j), 0 <= i <= j <= J
+__device__ __forceinline__ void pair_of(int e, int J, int &i, int &j) {
+  int off = 0;
+  i = 0;
+  while (off + (J + 1 - i) <= e) {
+    off += J + 1 - i;
+    ++i;
+  }
+  j = i + (e - off);
+}
+
+__device__ void load_system(const double *__restrict__ g, int J, int E, double lambda, double *A, double *b,
+                            int lane) {
+  for (int e = lane; e < E - 1; e += 32) {  // the last entry, sum x^2, is not part of the system
+    int i = 0, off = 0;
+    while (off + (J + 1 - i) <= e) {
+      off += J + 1 - i;
+      ++i;
+    }
+    const int j = i + (e - off);
+    const double v = g[e];
+    if (j == J) {
+      b[i] = v;
+    } else {
+      A[i * J + j] = v;
+      A[j * J + i] = v;
+    }
+  }
+  __syncwarp();
+  for (int i = lane; i < J; i += 32) A[i * J + i] += lambda;
+  __syncwarp();
+}
+
+// returns false when a pivot was not positive (A is left partly factored)
+__device__ bool cholesky_solve(double *A, double *b, int J, int lane) {
+  for (int k = 0; k < J; ++k) {
+    const double d = A[k * J + k];
+    if (!(d > 0.0) || !isfinite(d)) return false;  // uniform across the warp
+    const double lkk = sqrt(d);
+    __syncwarp();
+    for (int i = k + 1 + lane; i < J; i += 32) A[i * J + k] /= lkk;
+    if (lane == 0) A[k * J + k] = lkk;
+    __syncwarp();
+    for (int i = k + 1 + lane; i < J; i += 32) {
+      const double lik = A[i * J + k];
+      for (int j = k + 1; j <= i; ++j) A[i * J + j] -= lik * A[j * J + k];
+    }
+    __syncwarp();
+  }
+  for (int k = 0; k < J; ++k) {
+    const double yk = b[k] / A[k * J + k];
+    __syncwarp();
+    if (lane == 0) b[k] = yk;
+    for (int i = k + 1 + lane; i < J; i += 32) b[i] -= A[i * J + k] * yk;
+    __syncwarp();
+  }
+  for (int k = J - 1; k >= 0; --k) {
+    const double ak = b[k] / A[k * J + k];
+    __syncwarp();
+    if (lane == 0) b[k] = ak;
+    for (int i = lane; i < k; i += 32) b[i] -= A[k * J + i] * ak;
+    __syncwarp();
+  }
+  return true;
+}
+
+// LU with partial (row) pivoting, applied to b on the fly; returns false on an exactly zero pivot
+__device__ bool lu_solve(double *A, double *b, int J, int lane) {
+  bool ok = true;
+  for (int k = 0; k < J; ++k) {
+    double best = -1.0;
+    int bi = k;
+    for (int i = k + lane; i < J; i += 32) {
+      const double v = fabs(A[i * J + k]);
+      if (v > best) {
+        best = v;
+        bi = i;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+      const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+      if (ov > best || (ov == best && oi < bi)) {
+        best = ov;
+        bi = oi;
+      }
+    }
+    if (bi != k) {
+      for (int c = lane; c < J; c += 32) {
+        const double tmp = A[k * J + c];
+        A[k * J + c] = A[bi * J + c];
+        A[bi * J + c] = tmp;
+      }
+      if (lane == 0) {
+        const double tmp = b[k];
+        b[k] = b[bi];
+        b[bi] = tmp;
+      }
+    }
+    __syncwarp();
+    double d = A[k * J + k];
+    if (d == 0.0) {
+      ok = false;
+      d = 1e-300;
+    }
+    for (int i = k + 1 + lane; i < J; i += 32) {
+      const double f = A[i * J + k] / d;
+      A[i * J + k] = f;
+      for (int c = k + 1; c < J; ++c) A[i * J + c] -= f * A[k * J + c];
+      b[i] -= f * b[k];
+    }
+    __syncwarp();
+  }
+  for (int k = J - 1; k >= 0; --k) {
+    const double d = A[k * J + k];
+    const double xk = b[k] / (d == 0.0 ? 1e-300 : d);
+    __syncwarp();
+    if (lane == 0) b[k] = xk;
+    for (int i = lane; i < k; i += 32) b[i] -= A[i * J + k] * xk;
+    __syncwarp();
+  }
+  return ok;
+}
+
 template <class V>
 __global__ void k_solve(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf, V *__restrict__ fac,
-                        int *__restrict__ status, double lambda) {
+                        int *__restrict__ status, double lambda, double *__restrict__ err_partial) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   double *A = sm + (size_t)wib * ((size_t)J * J + J);
   double *b = A + (size_t)J * J;
+  double err = 0;  // sum over this warp's rows of sum_t (x_t - delta_t . a)^2
   for (uint64_t row = (uint64_t)blockIdx.x * wpb + wib; row < rows; row += (uint64_t)gridDim.x * wpb) {
     const double *g = gram + row * (uint64_t)E;
-    for (int e = lane; e < E; e += 32) {
-      int i = 0, off = 0;
-      while (off + (J + 1 - i) <= e) {
-        off += J + 1 - i;
-        ++i;
-      }
-      const int j = i + (e - off);
-      const double v = g[e];
-      if (j == J) {
-        b[i] = v;
-      } else {
-        A[i * J + j] = v;
-        A[j * J + i] = v;
-      }
-    }
-    __syncwarp();
-    for (int i = lane; i < J; i += 32) A[i * J + i] += lambda;
-    __syncwarp();
-    for (int k = 0; k < J; ++k) {
-      double d = A[k * J + k];
-      const bool bad = !(d > 0.0) || !isfinite(d);
-      if (bad) d = 1e-300;
-      const double lkk = sqrt(d);
+    load_system(g, J, E, lambda, A, b, lane);
+    if (!cholesky_solve(A, b, J, lane)) {
       __syncwarp();
-      for (int i = k + 1 + lane; i < J; i += 32) A[i * J + k] /= lkk;
-      if (lane == 0) {
-        A[k * J + k] = lkk;
-        if (bad) atomicOr(status, 1);
-      }
-      __syncwarp();
-      for (int i = k + 1 + lane; i < J; i += 32) {
-        const double lik = A[i * J + k];
-        for (int j = k + 1; j <= i; ++j) A[i * J + j] -= lik * A[j * J + k];
-      }
-      __syncwarp();
-    }
-    for (int k = 0; k < J; ++k) {
-      const double yk = b[k] / A[k * J + k];
-      __syncwarp();
-      if (lane == 0) b[k] = yk;
-      for (int i = k + 1 + lane; i < J; i += 32) b[i] -= A[i * J + k] * yk;
-      __syncwarp();
-    }
-    for (int k = J - 1; k >= 0; --k) {
-      const double ak = b[k] / A[k * J + k];
-      __syncwarp();
-      if (lane == 0) b[k] = ak;
-      for (int i = lane; i < k; i += 32) b[i] -= A[k * J + i] * ak;
-      __syncwarp();
+      load_system(g, J, E, lambda, A, b, lane);
+      const bool ok = lu_solve(A, b, J, lane);
+      if (lane == 0) atomicOr(status, ok ? 4 : 1);
     }
     V *frow = fac + row * (uint64_t)ldf;
     for (int j = lane; j < ldf; j += 32) frow[j] = j < J ? (V)b[j] : V(0);
+    if (err_partial) {
+      // with the stored (value_t) row a: sum x^2 - 2 a.C + a^T G a, G = B - lambda I
+      __syncwarp();
+      double e_row = 0;
+      for (int e = lane; e < E; e += 32) {
+        int i, j;
+        pair_of(e, J, i, j);
+        const double v = g[e];
+        if (i == J) {
+          e_row += v;
+        } else {
+          const double ai = (double)(V)b[i];
+          if (j == J)
+            e_row -= 2.0 * ai * v;
+          else
+            e_row += (i == j ? 1.0 : 2.0) * ai * (double)(V)b[j] * v;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) e_row += __shfl_xor_sync(0xFFFFFFFFu, e_row, o);
+      err += e_row;
+    }
     __syncwarp();
+  }
+  if (err_partial) {
+    __shared__ double werr[32];
+    if (lane == 0) werr[wib] = err;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0;
+      for (int w = 0; w < wpb; ++w) s += werr[w];
+      err_partial[blockIdx.x] = s;
+    }
   }
 }
 
@@ -544,8 +483,6 @@ struct Launch {
   bool spec = false;
 };
 
-inline int ldd_for(int J) { return ((J + 1) & 1) ? J + 1 : J + 2; }
-inline int pairs_for(int J) { return (J + 1) * (J + 2) / 2 - 1; }
 
 template <class V, int N, int J, int KIND> void spec_entry(Launch &L, const DevTensor &t) {
   constexpr int NPT = 2;
@@ -613,6 +550,7 @@ ModeArgs make_args(const DevTensor &t, int mode) {
   a.vperm = t.vperm[mode];
   a.gram = t.gram;
   a.partial = t.partial;
+  a.status = t.status;
   a.nnz = t.nnz;
   a.N = t.N;
   a.J = t.J;
@@ -697,7 +635,11 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   if (int rc = prof_begin(t, &ev)) return rc;
   GTK_CUDA(cudaMemsetAsync(t.gram, 0, t.rows[mode] * (uint64_t)E * 8, t.stream));
   if (t.nnz) {
-    if (int rc = launch_mode<V, kUpdate>(t, mode, nullptr, nullptr)) return rc;
+    if (t.precision != GTK_PREC_PLAIN) {
+      if (int rc = run_mode_tc(t, mode, 0, nullptr, nullptr)) return rc;
+    } else if (int rc = launch_mode<V, kUpdate>(t, mode, nullptr, nullptr)) {
+      return rc;
+    }
   }
   if (int rc = prof_end(t, 0, ev)) return rc;
   if (int rc = prof_begin(t, &ev)) return rc;
@@ -708,10 +650,18 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   if (int rc = prepare_fn((const void *)k_solve<V>, smem)) return rc;
   uint64_t grid = (t.rows[mode] + wpb - 1) / wpb;
   grid = std::min<uint64_t>(grid, (uint64_t)t.num_sms * 32);
+  // the last mode's Gram rows also give the fit of the sweep: its delta is built
+  // from the modes already updated in this sweep, so sum_t (x_t - delta_t . a_new)^2
+  // = sum x^2 - 2 a.C + a^T G a per row (reconstruction.cuh:259-268 without a
+  // second J^N pass over the nonzeros)
+  const bool last = mode == t.N - 1;
+  if (last) grid = std::min<uint64_t>(grid, kFitGridMax);
   if (grid < 1) grid = 1;
   k_solve<V><<<(unsigned)grid, wpb * 32, smem, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf, (V *)t.fac[mode],
-                                                           t.status, kLambda);
+                                                           t.status, kLambda, last ? t.partial : nullptr);
   GTK_CUDA(cudaGetLastError());
+  t.fit_from_gram = last;
+  t.fit_grid = (int)grid;
   if (int rc = prof_end(t, 1, ev)) return rc;
   return 0;
 }
@@ -724,8 +674,14 @@ template <class V> static int fit_impl(DevTensor &t, double *fit) {
   cudaEvent_t ev = nullptr;
   if (int rc = prof_begin(t, &ev)) return rc;
   int grid = 1;
-  if (t.nnz) {
-    if (int rc = launch_mode<V, kFit>(t, t.N - 1, nullptr, &grid)) return rc;
+  if (t.fit_from_gram) {
+    grid = t.fit_grid;  // the error partials of the last mode's solve
+  } else if (t.nnz) {
+    if (t.precision != GTK_PREC_PLAIN) {
+      if (int rc = run_mode_tc(t, t.N - 1, 1, nullptr, &grid)) return rc;
+    } else if (int rc = launch_mode<V, kFit>(t, t.N - 1, nullptr, &grid)) {
+      return rc;
+    }
   } else {
     GTK_CUDA(cudaMemsetAsync(t.partial, 0, 8, t.stream));
   }
@@ -735,6 +691,7 @@ template <class V> static int fit_impl(DevTensor &t, double *fit) {
   double err = 0;
   GTK_CUDA(cudaMemcpyAsync(&err, t.partial + kFitGridMax, 8, cudaMemcpyDeviceToHost, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
+  if (err < 0) err = 0;  // the Gram form can round below zero at a perfect fit
   *fit = (t.norm == 0) ? 1.0 : 1.0 - std::sqrt(err) / t.norm;
   return 0;
 }
@@ -743,6 +700,7 @@ int run_fit(DevTensor &t, double *fit) { return t.dtype == GTK_F32 ? fit_impl<fl
 
 int run_delta(DevTensor &t, int mode, void *d_out) {
   if (!t.nnz) return 0;
+  if (t.precision != GTK_PREC_PLAIN) return run_mode_tc(t, mode, 2, d_out, nullptr);
   return t.dtype == GTK_F32 ? launch_mode<float, kDelta>(t, mode, d_out, nullptr)
                             : launch_mode<double, kDelta>(t, mode, d_out, nullptr);
 }

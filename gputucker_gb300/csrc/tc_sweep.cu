@@ -1,0 +1,440 @@
+// tc_sweep.cu -- the mode update and the fit with the delta contraction on the
+// 5th-generation tensor cores (tcgen05, TMEM accumulators), BF16 or TF32 inputs,
+// FP32 accumulation.  The precision form of the sweep; the plain form is sweep.cu.
+//
+// For mode n with other modes o_1 < ... < o_D (D = N-1 = 2 or 3), per nonzero t:
+//   K_t[(j, l)]      = a_{o_{D-1}}[t, j] * a_{o_D}[t, l]                 (J^2, SIMT)
+//   T[t, c]          = sum_k K_t[k] * G_n[c, k]      c = (j_n[, j_1])    (tcgen05 GEMM)
+//   delta_t[j_n]     = T[t, j_n]                                  (D = 2)
+//                    = sum_{j_1} a_{o_1}[t, j_1] * T[t, (j_n, j_1)]  (D = 3, SIMT)
+// A tile = 128 nonzeros x K (K = J^2 padded to 16), B = G_n [J^(D-1) padded to 16] x K,
+// both K-major in the canonical no-swizzle layout (8-row x 16-byte core matrices,
+// K-adjacent core matrices 128 B apart, 8-row groups K*2 B / K*4 B apart).  One
+// thread issues the MMAs (K/16 of them for BF16, K/8 for TF32) into a TMEM
+// accumulator of 128 lanes x N columns; each warp reads its 32 lanes back with
+// tcgen05.ld, finishes delta in registers and hands it to the same row-segmented
+// Gram/RHS reduction as the plain kernel.
+//
+// Every wait on the MMA-completion mbarrier is bounded: on timeout the CTA sets
+// bit 1 of the status word, frees its TMEM and returns.
+
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "internal.h"
+#include "mode_common.cuh"
+
+namespace gtk {
+namespace {
+
+constexpr int kTcThreads = 128;  // 4 warps; thread t owns TMEM lane t = nonzero t of the tile
+constexpr int kTcFitGrid = 1024;
+constexpr uint32_t kWaitLimit = 1u << 24;
+
+// ---------------------------------------------------------------- PTX wrappers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_alloc(uint32_t *slot, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(slot)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+template <int PREC>
+__device__ __forceinline__ void mma(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+  if (PREC == GTK_PREC_BF16) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+  } else {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+  }
+}
+__device__ __forceinline__ void mma_commit(uint64_t *bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// shared-memory matrix descriptor: K-major, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+  d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1 << 46;  // descriptor version of sm_100 family
+  return d;              // base offset 0, absolute LBO mode, layout type 0 = no swizzle
+}
+
+// instruction descriptor: D = F32, A/B = BF16 (kind::f16) or TF32 (kind::tf32), both K-major
+__host__ __device__ constexpr uint32_t instr_desc(int prec, int M, int N) {
+  return (1u << 4) | ((uint32_t)(prec == GTK_PREC_BF16 ? 1 : 2) << 7) |
+         ((uint32_t)(prec == GTK_PREC_BF16 ? 1 : 2) << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return r;
+}
+
+// 16 bytes of one core-matrix row from consecutive K values v[0..epc)
+template <int PREC> __device__ __forceinline__ uint4 pack16(const float *v);
+template <> __device__ __forceinline__ uint4 pack16<GTK_PREC_BF16>(const float *v) {
+  uint4 u;
+  __nv_bfloat162 h;
+  h = __floats2bfloat162_rn(v[0], v[1]);
+  u.x = *reinterpret_cast<uint32_t *>(&h);
+  h = __floats2bfloat162_rn(v[2], v[3]);
+  u.y = *reinterpret_cast<uint32_t *>(&h);
+  h = __floats2bfloat162_rn(v[4], v[5]);
+  u.z = *reinterpret_cast<uint32_t *>(&h);
+  h = __floats2bfloat162_rn(v[6], v[7]);
+  u.w = *reinterpret_cast<uint32_t *>(&h);
+  return u;
+}
+template <> __device__ __forceinline__ uint4 pack16<GTK_PREC_TF32>(const float *v) {
+  return make_uint4(to_tf32(v[0]), to_tf32(v[1]), to_tf32(v[2]), to_tf32(v[3]));
+}
+
+template <int J, int D, int PREC> struct TcShape {
+  static constexpr int ES = PREC == GTK_PREC_BF16 ? 2 : 4;  // element bytes
+  static constexpr int EPC = 16 / ES;                       // elements per 16-byte core row
+  static constexpr int KSTEP = 32 / ES;                     // K per MMA instruction (32 bytes)
+  static constexpr int KD = J * J;
+  static constexpr int KP = (KD + 15) / 16 * 16;
+  static constexpr int ND = D == 3 ? J * J : J;
+  static constexpr int NP = (ND + 15) / 16 * 16 < 16 ? 16 : (ND + 15) / 16 * 16;
+  static constexpr int NCOLS = NP <= 32 ? 32 : NP <= 64 ? 64 : NP <= 128 ? 128 : NP <= 256 ? 256 : 512;
+  static constexpr int SBO = (KP / EPC) * 128;  // bytes between 8-row groups
+  static constexpr int A_BYTES = kTcThreads * KP * ES;
+  static constexpr int B_BYTES = NP * KP * ES;
+  static constexpr int LDD = ((J + 1) & 1) ? J + 1 : J + 2;
+  static constexpr int E = (J + 1) * (J + 2) / 2;
+  static constexpr int OFF_B = A_BYTES;
+  static constexpr int OFF_DX = (OFF_B + B_BYTES + 15) / 16 * 16;
+  static constexpr int OFF_ROWS = OFF_DX + (kTcThreads * LDD * 4 + 15) / 16 * 16;
+  static constexpr int OFF_SEG = OFF_ROWS + kTcThreads * 4;
+  static constexpr int OFF_PAIRS = OFF_SEG + ((kTcThreads + 1) * 4 + 15) / 16 * 16;
+  static constexpr int OFF_BAR = OFF_PAIRS + (2 * E + 15) / 16 * 16;
+  static constexpr int OFF_SLOT = OFF_BAR + 16;
+  static constexpr int SMEM = OFF_SLOT + 16;
+};
+
+__device__ __forceinline__ uint32_t canon_off(int r, int k, int sbo, int es) {
+  const int epc = 16 / es;
+  return (uint32_t)((r >> 3) * sbo + (k / epc) * 128 + (r & 7) * 16 + (k % epc) * es);
+}
+
+template <int J, int D, int PREC, int KIND>
+__global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
+  using S = TcShape<J, D, PREC>;
+  constexpr int LDG = (J + 3) / 4 * 4;  // factor row stride (floats)
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t *bar = reinterpret_cast<uint64_t *>(smem + S::OFF_BAR);
+  uint32_t *slot = reinterpret_cast<uint32_t *>(smem + S::OFF_SLOT);
+  const int tid = threadIdx.x, warp = tid >> 5;
+  TileSmem<float> ts;
+  ts.gp = nullptr;
+  ts.arow = nullptr;
+  ts.dx = reinterpret_cast<float *>(smem + S::OFF_DX);
+  ts.rows = reinterpret_cast<uint32_t *>(smem + S::OFF_ROWS);
+  ts.seg = reinterpret_cast<uint32_t *>(smem + S::OFF_SEG);
+  ts.pi = smem + S::OFF_PAIRS;
+  ts.pj = smem + S::OFF_PAIRS + S::E;
+
+  if (warp == 0) {
+    tmem_alloc(slot, S::NCOLS);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    mbar_init(bar, 1);
+    fence_mbar_init();
+  }
+  // B = G_n as [N rows (j_n[, j_1])] x [K (j, l)], zero padded
+  {
+    const float *gp = reinterpret_cast<const float *>(a.corep);
+    for (int idx = tid; idx < S::NP * (S::KP / S::EPC); idx += kTcThreads) {
+      const int n = idx / (S::KP / S::EPC), c = idx % (S::KP / S::EPC);
+      float v[8];
+#pragma unroll
+      for (int e = 0; e < S::EPC; ++e) {
+        const int k = c * S::EPC + e;
+        v[e] = (n < S::ND && k < S::KD) ? gp[(size_t)(n * J + k / J) * LDG + (k % J)] : 0.f;
+      }
+      *reinterpret_cast<uint4 *>(smem + S::OFF_B + canon_off(n, c * S::EPC, S::SBO, S::ES)) = pack16<PREC>(v);
+    }
+  }
+  if (KIND == 0) fill_pairs(ts.pi, ts.pj, J);
+  fence_proxy_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *slot;
+  const uint32_t a_base = smem_u32(smem), b_base = smem_u32(smem + S::OFF_B);
+  constexpr uint32_t IDESC = instr_desc(PREC, 128, S::NP);
+  const float *facn = reinterpret_cast<const float *>(a.fac[a.mode]);
+  double err = 0;
+  uint32_t phase = 0;
+  bool timed_out = false;
+  const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const uint64_t t0 = tile * kTcThreads;
+    const int nv = (int)min((uint64_t)kTcThreads, a.nnz - t0);
+    const bool valid = tid < nv;
+    const uint64_t gi = valid ? t0 + tid : t0;
+    const uint32_t row = valid ? a.coord[a.mode][gi] : 0xFFFFFFFFu;
+    const float x = valid ? reinterpret_cast<const float *>(a.val)[gi] : 0.f;
+    // factor rows: p, q form the Kronecker operand; e (D = 3) finishes the contraction
+    float p[LDG], q[LDG], e1[LDG];
+    {
+      const float4 *fp = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 2]]) +
+                                                          (size_t)a.coord[a.others[D - 2]][gi] * LDG);
+      const float4 *fq = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 1]]) +
+                                                          (size_t)a.coord[a.others[D - 1]][gi] * LDG);
+#pragma unroll
+      for (int c = 0; c < LDG / 4; ++c) {
+        const float4 u = __ldg(fp + c), w = __ldg(fq + c);
+        p[4 * c] = u.x, p[4 * c + 1] = u.y, p[4 * c + 2] = u.z, p[4 * c + 3] = u.w;
+        q[4 * c] = w.x, q[4 * c + 1] = w.y, q[4 * c + 2] = w.z, q[4 * c + 3] = w.w;
+      }
+      if (D == 3) {
+        const float4 *fe = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[0]]) +
+                                                            (size_t)a.coord[a.others[0]][gi] * LDG);
+#pragma unroll
+        for (int c = 0; c < LDG / 4; ++c) {
+          const float4 u = __ldg(fe + c);
+          e1[4 * c] = u.x, e1[4 * c + 1] = u.y, e1[4 * c + 2] = u.z, e1[4 * c + 3] = u.w;
+        }
+      }
+    }
+    // A row `tid`: the Kronecker product p (x) q, rounded to the MMA input type
+#pragma unroll
+    for (int c = 0; c < S::KP / S::EPC; ++c) {
+      float v[8];
+#pragma unroll
+      for (int e = 0; e < S::EPC; ++e) {
+        const int k = c * S::EPC + e;
+        v[e] = k < S::KD ? p[k / J] * q[k % J] : 0.f;
+      }
+      *reinterpret_cast<uint4 *>(smem + canon_off(tid, c * S::EPC, S::SBO, S::ES)) = pack16<PREC>(v);
+    }
+    fence_proxy_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      tc_fence_after();
+#pragma unroll
+      for (int s = 0; s < S::KP / S::KSTEP; ++s)
+        mma<PREC>(tmem, smem_desc(a_base + s * 256, 128, S::SBO), smem_desc(b_base + s * 256, 128, S::SBO), IDESC,
+                  s > 0 ? 1u : 0u);
+      mma_commit(bar);
+    }
+    uint32_t spins = 0;
+    bool done = false;
+    while (!(done = mbar_try_wait(bar, phase)) && ++spins < kWaitLimit) {
+    }
+    timed_out = __syncthreads_or(done ? 0 : 1) != 0;  // the whole CTA agrees
+    if (timed_out) {
+      if (tid == 0) atomicOr(a.status, 2);
+      break;
+    }
+    phase ^= 1u;
+    tc_fence_after();
+    // epilogue: delta from this thread's TMEM lane
+    float delta[J];
+#pragma unroll
+    for (int j = 0; j < J; ++j) delta[j] = 0.f;
+#pragma unroll
+    for (int c = 0; c < S::NP / 16; ++c) {
+      float v[16];
+      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+      tmem_wait_ld();
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        const int col = c * 16 + i;
+        if (col < S::ND) {
+          if (D == 2)
+            delta[col] = v[i];
+          else
+            delta[col / J] += e1[col % J] * v[i];
+        }
+      }
+    }
+    tc_fence_before();
+    if (KIND == 0) {
+#pragma unroll
+      for (int j = 0; j < J; ++j) ts.dx[tid * S::LDD + j] = delta[j];
+      ts.dx[tid * S::LDD + J] = x;
+      ts.rows[tid] = row;
+      __syncthreads();
+      gram_phase<float>(a, ts, t0, nv, 1);
+      __syncthreads();
+    } else if (KIND == 1) {
+      if (valid) {
+        float xh = 0.f;
+#pragma unroll
+        for (int j = 0; j < J; ++j) xh += delta[j] * __ldg(facn + (size_t)row * LDG + j);
+        const float d = x - xh;
+        err += (double)d * (double)d;
+      }
+      __syncthreads();
+    } else {
+      if (valid) {
+        float *out = reinterpret_cast<float *>(a.out) + (size_t)a.vperm[gi] * J;
+#pragma unroll
+        for (int j = 0; j < J; ++j) out[j] = delta[j];
+      }
+      __syncthreads();
+    }
+  }
+  if (KIND == 1) {
+    const double tot = block_sum(err);
+    if (tid == 0) a.partial[blockIdx.x] = tot;
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, S::NCOLS);
+  }
+}
+
+struct TcLaunch {
+  const void *fn = nullptr;
+  int smem = 0, ncols = 0;
+};
+
+template <int J, int D, int PREC, int KIND> TcLaunch tc_entry() {
+  using S = TcShape<J, D, PREC>;
+  TcLaunch L;
+  L.fn = (const void *)k_mode_tc<J, D, PREC, KIND>;
+  L.smem = S::SMEM;
+  L.ncols = S::NCOLS;
+  return L;
+}
+
+// (N, J) shapes with a tensor-core form
+template <int PREC, int KIND> bool tc_find(TcLaunch &L, int N, int J) {
+#define GTK_TC(NN, JJ)                             \
+  if (N == NN && J == JJ) {                        \
+    L = tc_entry<JJ, NN - 1, PREC, KIND>();        \
+    return true;                                   \
+  }
+  GTK_TC(3, 4) GTK_TC(3, 8) GTK_TC(3, 10) GTK_TC(3, 12) GTK_TC(3, 16)
+  GTK_TC(4, 4) GTK_TC(4, 8) GTK_TC(4, 10) GTK_TC(4, 12)
+#undef GTK_TC
+  return false;
+}
+
+template <int KIND> bool tc_choose(TcLaunch &L, int prec, int N, int J) {
+  return prec == GTK_PREC_BF16 ? tc_find<GTK_PREC_BF16, KIND>(L, N, J) : tc_find<GTK_PREC_TF32, KIND>(L, N, J);
+}
+
+int tc_prepare(const TcLaunch &L, int num_sms, int *grid_cap, int *smem_out) {
+  // at most 512 / ncols CTAs may share an SM's TMEM: request enough shared
+  // memory that no more than that many fit, so tcgen05.alloc never has to wait
+  const int max_ctas = 512 / L.ncols;
+  const int sm_bytes = 233472;  // 228 KB of shared memory per SM
+  int smem = L.smem;
+  if ((smem + 1024) * (max_ctas + 1) <= sm_bytes) smem = sm_bytes / (max_ctas + 1) - 1024 + 16;
+  GTK_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+  int per_sm = 0;
+  GTK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, kTcThreads, smem));
+  if (per_sm < 1) return fail(GTK_ERR_UNSUPPORTED, "tensor-core mode kernel does not fit on an SM");
+  if (per_sm > max_ctas) return fail(GTK_ERR_UNSUPPORTED, "tensor-core kernel would oversubscribe TMEM");
+  *grid_cap = per_sm * num_sms;
+  *smem_out = smem;
+  return 0;
+}
+
+}  // namespace
+
+bool tc_supported(int N, int J, int dtype) {
+  TcLaunch L;
+  return dtype == GTK_F32 && tc_choose<0>(L, GTK_PREC_BF16, N, J);
+}
+
+// kind 0 update (Gram/RHS into t.gram), 1 fit (partials), 2 delta (out)
+int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
+  TcLaunch L;
+  const bool ok = kind == 0   ? tc_choose<0>(L, t.precision, t.N, t.J)
+                  : kind == 1 ? tc_choose<1>(L, t.precision, t.N, t.J)
+                              : tc_choose<2>(L, t.precision, t.N, t.J);
+  if (!ok || t.dtype != GTK_F32) return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this shape");
+  int cap = 0, smem = 0;
+  if (int rc = tc_prepare(L, t.num_sms, &cap, &smem)) return rc;
+  ModeArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int k = 0; k < t.N; ++k) {
+    a.coord[k] = t.vidx[mode][k];
+    a.fac[k] = t.fac[k];
+  }
+  a.val = t.vval[mode];
+  a.corep = t.corep[mode];
+  a.vperm = t.vperm[mode];
+  a.out = out;
+  a.gram = t.gram;
+  a.partial = t.partial;
+  a.status = t.status;
+  a.nnz = t.nnz;
+  a.N = t.N;
+  a.J = t.J;
+  a.ldf = t.ldf;
+  a.mode = mode;
+  a.E = pairs_for(t.J);
+  a.ldd = ldd_for(t.J);
+  int m = 0;
+  for (int k = 0; k < t.N; ++k)
+    if (k != mode) a.others[m++] = k;
+  const uint64_t ntiles = (t.nnz + kTcThreads - 1) / kTcThreads;
+  uint64_t grid = std::min<uint64_t>(ntiles, (uint64_t)cap);
+  if (kind == 1) grid = std::min<uint64_t>(grid, kTcFitGrid);
+  if (grid < 1) grid = 1;
+  void *args[] = {&a};
+  GTK_CUDA(cudaLaunchKernel(L.fn, dim3((unsigned)grid), dim3(kTcThreads), args, (size_t)smem, t.stream));
+  if (grid_used) *grid_used = (int)grid;
+  return 0;
+}
+
+}  // namespace gtk
