@@ -248,8 +248,8 @@ def main():
     k_ms, k_n = t.profile_read(0)
     s_ms, s_n = t.profile_read(1)
     f_ms, f_n = t.profile_read(2)
+    launches = int(t.profile_read(4)[1])  # kernels the library launched in the timed region
     t.profile(False)
-    launches = int(k_n + s_n + f_n)  # fused + solve per mode; the fit is one final sum (its error comes from the last solve)
     ms_step = ms / args.steps
     value = dist.world * N * nnz * args.steps / (ms / 1e3)
     # ---- roofline of the dominant kernel (fused delta + Gram/RHS)
@@ -274,10 +274,17 @@ def main():
         pass
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
-        "traffic": traffic, "kernel": "k_mode_spec<float,4,10,2,kUpdate> (fused delta + Gram/RHS)",
+        "traffic": traffic,
+        "kernel": ("k_mode_spec<float,4,10,2,kUpdate>" if args.precision == "plain"
+                   else f"k_mode_tc<10,3,{args.precision},update>") + " (fused delta + Gram/RHS)",
         "bytes_per_launch": bytes_per_launch, "launch_ms": per_launch_s * 1e3,
         "fp32_tflops": nnz * flops_delta / per_launch_s / 1e12, "fp32_peak_tflops_nominal": 80.6,
         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
+    }
+    kernels = {
+        "delta_gram": {"launches": k_n, "ms_per_launch": k_ms / max(1, k_n)},
+        "row_solve": {"launches": s_n, "ms_per_launch": s_ms / max(1, s_n)},
+        "fit": {"launches": f_n, "ms_per_launch": f_ms / max(1, f_n)},
     }
     t.close()
     # ---- end to end through the C ABI with host buffers
@@ -320,7 +327,9 @@ def main():
             | {"nnz": nnz, "parallelism": f"replicas{dist.world}", "l2": "inputs (8 GB views) exceed the 129 MB L2",
                "generator_s": gen_s},
             "fit_last": fits[-1] if fits else None,
+            "fits": [round(f, 6) for f in fits],
             "gpu_launches": launches,
+            "kernels": kernels,
             "roofline": roofline,
             "e2e": e2e,
             "cpu_baseline": cpu,

@@ -70,7 +70,7 @@ static void release(DevTensor &t) {
 
 // slab layout [rows][J] <-> device [rows][ldf]
 static int put_factor(DevTensor &t, int n, const void *slabs) {
-  t.fit_from_gram = false;
+  t.fit_from_store = false;
   GTK_CUDA(cudaMemcpy2DAsync(t.fac[n], (size_t)t.ldf * t.vsize, slabs, (size_t)t.J * t.vsize, (size_t)t.J * t.vsize,
                              t.rows[n], cudaMemcpyHostToDevice, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
@@ -85,7 +85,7 @@ static int get_factor(const DevTensor &t, int n, void *slabs) {
 }
 
 static int put_core(DevTensor &t, const void *core) {
-  t.fit_from_gram = false;
+  t.fit_from_store = false;
   GTK_CUDA(cudaMemcpyAsync(t.core, core, t.core_n * t.vsize, cudaMemcpyHostToDevice, t.stream));
   if (int rc = upload_core_perms(t, core)) return rc;
   t.have_core = true;
@@ -263,7 +263,7 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
   t->J = rank;
   const int w = (int)(16 / t->vsize);
   t->ldf = (rank + w - 1) / w * w;
-  t->E = (rank + 1) * (rank + 2) / 2;
+  t->E = (rank + 1) * (rank + 2) / 2 - 1;
   t->nnz = coo->nnz;
   t->nblk = nblk;
   t->core_n = core_n;
@@ -308,6 +308,8 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
   A((void **)&t->gram, max_rows * (uint64_t)t->E * 8);
   A((void **)&t->partial, kPartialDoubles * 8);
   A((void **)&t->status, 16);
+  A((void **)&t->fallback, max_rows * 4);
+  A((void **)&t->nfallback, 16);
   if (rc) return bail(rc);
   for (int n = 0; n < N; ++n) {
     if ((rc = ck(cudaMemsetAsync(t->fac[n], 0, t->rows[n] * t->ldf * vs, t->stream), "memset"))) return bail(rc);
@@ -464,7 +466,7 @@ int gtk_set_precision(gtk_tensor *t, int precision) {
   if (!t) return fail(GTK_ERR_ARG, "null tensor");
   if (precision != GTK_PREC_PLAIN && precision != GTK_PREC_BF16 && precision != GTK_PREC_TF32)
     return fail(GTK_ERR_ARG, "unknown precision");
-  t->fit_from_gram = false;
+  t->fit_from_store = false;
   if (precision != GTK_PREC_PLAIN && !tc_supported(t->N, t->J, t->dtype))
     return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this order/rank/value type (FP32, N = 3 or 4, "
                                      "J in {4, 8, 10, 12, 16} for N = 3 and {4, 8, 10, 12} for N = 4)");
@@ -551,7 +553,12 @@ int gtk_profile_enable(gtk_tensor *t, int on) {
 }
 
 int gtk_profile_read(gtk_tensor *t, int kind, double *ms, uint64_t *launches) {
-  if (!t || kind < 0 || kind > 3) return fail(GTK_ERR_ARG, "bad argument");
+  if (!t || kind < 0 || kind > 4) return fail(GTK_ERR_ARG, "bad argument");
+  if (kind == 4) {  // kernels launched by the sweep entry points since the last reset
+    if (ms) *ms = 0;
+    if (launches) *launches = t->launches;
+    return 0;
+  }
   if (int rc = set_dev(t)) return rc;
   if (int rc = prof_resolve(*t)) return rc;
   double m = 0;
@@ -577,6 +584,7 @@ int gtk_profile_reset(gtk_tensor *t) {
     t->prof_ms[k] = 0;
     t->prof_n[k] = 0;
   }
+  t->launches = 0;
   return 0;
 }
 

@@ -60,11 +60,12 @@ struct Xoshiro {  // xoshiro256**
   }
 };
 
-unsigned threads_for(uint64_t work) {
+// threads for `tasks` independent work items (chunks or buckets)
+unsigned threads_for(uint64_t tasks) {
   unsigned nt = std::thread::hardware_concurrency();
   if (nt == 0) nt = 1;
   nt = std::min<unsigned>(nt, 64);
-  return (unsigned)std::min<uint64_t>(nt, work / 65536 + 1);
+  return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(nt, tasks));
 }
 
 template <class F> void parallel_for(uint64_t n, F f) {
@@ -163,22 +164,36 @@ int generate(int N, const uint32_t *dims, uint64_t nnz, int index_dist, double z
     std::vector<const uint32_t *> ip(N);
     for (int n = 0; n < N; ++n) ip[n] = cand[n].data();
     std::vector<uint32_t> bucket_of(total);
-    std::vector<std::vector<uint64_t>> counts(threads_for(total), std::vector<uint64_t>(B, 0));
-    std::vector<uint64_t> start(B + 1, 0);
-    {
-      std::vector<uint32_t> cnt(B, 0);
-      for (uint64_t t = 0; t < total; ++t) {
-        uint32_t b = (uint32_t)(tuple_hash(ip.data(), N, t) % B);
+    const uint64_t nchunk = (total + kChunk - 1) / kChunk;
+    std::vector<uint64_t> hist(nchunk * B, 0);  // [chunk][bucket]
+    parallel_for(nchunk, [&](uint64_t c) {
+      uint64_t *h = &hist[c * B];
+      const uint64_t e = std::min(total, (c + 1) * kChunk);
+      for (uint64_t t = c * kChunk; t < e; ++t) {
+        const uint32_t b = (uint32_t)(tuple_hash(ip.data(), N, t) % B);
         bucket_of[t] = b;
-        ++cnt[b];
+        ++h[b];
       }
-      for (uint32_t b = 0; b < B; ++b) start[b + 1] = start[b] + cnt[b];
+    });
+    // slot of (bucket, chunk): buckets in order, chunks in order inside a bucket
+    std::vector<uint64_t> start(B + 1, 0), base(nchunk * B);
+    {
+      uint64_t pos = 0;
+      for (uint32_t b = 0; b < B; ++b) {
+        start[b] = pos;
+        for (uint64_t c = 0; c < nchunk; ++c) {
+          base[c * B + b] = pos;
+          pos += hist[c * B + b];
+        }
+      }
+      start[B] = pos;
     }
     std::vector<uint32_t> order(total);
-    {
-      std::vector<uint64_t> fillp(start.begin(), start.end() - 1);
-      for (uint64_t t = 0; t < total; ++t) order[fillp[bucket_of[t]]++] = (uint32_t)t;
-    }
+    parallel_for(nchunk, [&](uint64_t c) {
+      uint64_t *bp = &base[c * B];
+      const uint64_t e = std::min(total, (c + 1) * kChunk);
+      for (uint64_t t = c * kChunk; t < e; ++t) order[bp[bucket_of[t]]++] = (uint32_t)t;
+    });
     keep.assign(total, 0);
     parallel_for(B, [&](uint64_t b) {
       uint32_t *s = order.data() + start[b], *e = order.data() + start[b + 1];
@@ -200,7 +215,16 @@ int generate(int N, const uint32_t *dims, uint64_t nnz, int index_dist, double z
       }
     });
     distinct = 0;
-    for (uint64_t t = 0; t < total; ++t) distinct += keep[t];
+    {
+      std::vector<uint64_t> part(nchunk, 0);
+      parallel_for(nchunk, [&](uint64_t c) {
+        const uint64_t e = std::min(total, (c + 1) * kChunk);
+        uint64_t k = 0;
+        for (uint64_t t = c * kChunk; t < e; ++t) k += keep[t];
+        part[c] = k;
+      });
+      for (uint64_t k : part) distinct += k;
+    }
     if (distinct >= nnz) break;
     M = total + (total - distinct) * 2 + (nnz - distinct) * 2;
   }
@@ -210,18 +234,39 @@ int generate(int N, const uint32_t *dims, uint64_t nnz, int index_dist, double z
   out->nnz = nnz;
   for (int n = 0; n < N; ++n) out->idx[n].resize(nnz);
   {
-    uint64_t k = 0;
-    for (uint64_t t = 0; k < nnz; ++t) {
-      if (!keep[t]) continue;
-      for (int n = 0; n < N; ++n) out->idx[n][k] = cand[n][t];
-      ++k;
-    }
+    // the first nnz kept candidates, in draw order; chunk offsets make it parallel
+    const uint64_t total = keep.size(), nchunk = (total + kChunk - 1) / kChunk;
+    std::vector<uint64_t> off(nchunk + 1, 0);
+    parallel_for(nchunk, [&](uint64_t c) {
+      uint64_t k = 0;
+      const uint64_t e = std::min(total, (c + 1) * kChunk);
+      for (uint64_t t = c * kChunk; t < e; ++t) k += keep[t];
+      off[c + 1] = k;
+    });
+    for (uint64_t c = 0; c < nchunk; ++c) off[c + 1] += off[c];
+    parallel_for(nchunk, [&](uint64_t c) {
+      uint64_t k = off[c];
+      const uint64_t e = std::min(total, (c + 1) * kChunk);
+      for (uint64_t t = c * kChunk; t < e && k < nnz; ++t) {
+        if (!keep[t]) continue;
+        for (int n = 0; n < N; ++n) out->idx[n][k] = cand[n][t];
+        ++k;
+      }
+    });
   }
   cand.clear();
   for (int n = 0; n < N; ++n) {
-    uint32_t mx = 0;
-    for (uint64_t k = 0; k < nnz; ++k) mx = std::max(mx, out->idx[n][k]);
-    out->dims[n] = nnz ? mx + 1 : 0;
+    const uint64_t nchunk = (nnz + kChunk - 1) / kChunk;
+    std::vector<uint32_t> mx(nchunk + 1, 0);
+    parallel_for(nchunk, [&](uint64_t c) {
+      const uint64_t e = std::min(nnz, (c + 1) * kChunk);
+      uint32_t m = 0;
+      for (uint64_t k = c * kChunk; k < e; ++k) m = std::max(m, out->idx[n][k]);
+      mx[c] = m;
+    });
+    uint32_t m = 0;
+    for (uint32_t x : mx) m = std::max(m, x);
+    out->dims[n] = nnz ? m + 1 : 0;
   }
   // values
   const uint64_t vseed = splitmix(sseed);
@@ -279,7 +324,10 @@ int generate(int N, const uint32_t *dims, uint64_t nnz, int index_dist, double z
   }
   if (dtype == GTK_F32) {
     out->vf.resize(nnz);
-    for (uint64_t t = 0; t < nnz; ++t) out->vf[t] = (float)v[t];
+    parallel_for((nnz + kChunk - 1) / kChunk, [&](uint64_t c) {
+      const uint64_t e = std::min(nnz, (c + 1) * kChunk);
+      for (uint64_t t = c * kChunk; t < e; ++t) out->vf[t] = (float)v[t];
+    });
   } else {
     out->vd = std::move(v);
   }

@@ -123,8 +123,12 @@ struct DevTensor {
   int *status = nullptr;      // device status words (numeric flags)
   int num_sms = 0;
   uint64_t lu_fallbacks = 0;
-  bool fit_from_gram = false;  // partials hold the fit error of the last mode's update
-  int fit_grid = 0;  // sweeps in which some row needed the pivoted-LU fallback
+  bool fit_from_store = false;  // dstore holds the delta of the last mode's update
+  bool dstore_failed = false;
+  void *dstore = nullptr;       // [nnz][J] value_t, view order of the last mode
+  uint32_t *fallback = nullptr; // rows re-solved by pivoted LU
+  unsigned int *nfallback = nullptr;
+  uint64_t launches = 0;        // kernels launched by the sweep entry points  // sweeps in which some row needed the pivoted-LU fallback
 
   // profiling
   bool prof = false;

@@ -30,6 +30,7 @@ struct ModeArgs {
   double *gram;                      // kUpdate: [rows][E]
   double *partial;                   // kFit: per-CTA error sums
   int *status;                       // device status word (bit 1: a bounded wait gave up)
+  void *dstore;                      // kUpdate: when set, delta of every nonzero in view order [nnz][J]
   uint64_t nnz;
   int N, J, ldf, mode, E, ldd;
   int others[kMaxOrder];             // the other modes in increasing order
@@ -95,15 +96,15 @@ __device__ TileSmem<V> carve(unsigned char *base, size_t gp_elems, int arow_leve
   return s;
 }
 
-// pair table of the Gram/RHS entries: e -> (i, j), 0 <= i <= j <= J, row-major
-// over the upper triangle.  Column J of the delta tile holds x, so (i, J) is the
-// right-hand side C_i = sum x*delta_i and the last entry (J, J) is sum x^2 of the
-// row, which the fit uses (sum (x - delta.a)^2 = sum x^2 - 2 a.C + a^T G a).
+// pair table of the Gram/RHS entries: e -> (i, j), i <= j <= J, except (J, J),
+// row-major over the upper triangle.  Column J of the delta tile holds x, so
+// (i, J) is the right-hand side C_i = sum x*delta_i.
 __device__ void fill_pairs(unsigned char *pi, unsigned char *pj, int J) {
   if (threadIdx.x == 0) {
     int e = 0;
     for (int i = 0; i <= J; ++i)
       for (int j = i; j <= J; ++j) {
+        if (i == J && j == J) continue;
         pi[e] = (unsigned char)i;
         pj[e] = (unsigned char)j;
         ++e;
@@ -198,6 +199,54 @@ __device__ void gram_phase(const ModeArgs &a, const TileSmem<V> &s, uint64_t til
 }
 
 
+// Running Gram/RHS sums of one warp.  Lane l owns the entries e = l + 32k
+// (k < KE) of the packed row; the warp walks its slice of each tile in view
+// order, adding delta_i * delta_j (rounded to value_t) for every entry, and
+// flushes its sums with FP64 atomics whenever the row changes and at the end
+// of the CTA's (contiguous) range of tiles.  A long row thus costs one flush
+// per warp and CTA, a short row one or two flushes; no block-wide barrier is
+// needed inside the reduction.
+template <class V, int KE> struct GramAcc {
+  ProdSum<V> acc[KE];
+  int ei[KE], ej[KE];
+  uint32_t row = 0xFFFFFFFFu;
+
+  __device__ void init(const unsigned char *pi, const unsigned char *pj, int E, int lane) {
+#pragma unroll
+    for (int k = 0; k < KE; ++k) {
+      const int e = lane + 32 * k;
+      ei[k] = e < E ? pi[e] : -1;
+      ej[k] = e < E ? pj[e] : 0;
+      acc[k] = ProdSum<V>();
+    }
+  }
+  __device__ void flush(double *gram, int E, int lane) {
+    if (row != 0xFFFFFFFFu) {
+#pragma unroll
+      for (int k = 0; k < KE; ++k)
+        if (ei[k] >= 0) atomicAdd(gram + (size_t)row * E + lane + 32 * k, acc[k].value());
+    }
+#pragma unroll
+    for (int k = 0; k < KE; ++k) acc[k] = ProdSum<V>();
+  }
+  // tile positions [t0, t1) of the shared delta tile (row stride ldd, column J = x)
+  __device__ void run(const V *dx, int ldd, const uint32_t *rows, int t0, int t1, double *gram, int E, int lane) {
+    for (int t = t0; t < t1; ++t) {
+      const uint32_t r = rows[t];
+      if (r != row) {
+        flush(gram, E, lane);
+        row = r;
+      }
+      const V *d = dx + t * ldd;
+#pragma unroll
+      for (int k = 0; k < KE; ++k)
+        if (ei[k] >= 0) acc[k].add(mul_rn(d[ei[k]], d[ej[k]]));
+    }
+  }
+};
+
+__host__ __device__ constexpr int gram_slots(int J) { return ((J + 1) * (J + 2) / 2 - 1 + 31) / 32; }
+
 __device__ inline double block_sum(double v) {
   __shared__ double sw[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -214,7 +263,7 @@ __device__ inline double block_sum(double v) {
 
 
 inline int ldd_for(int J) { return ((J + 1) & 1) ? J + 1 : J + 2; }
-inline int pairs_for(int J) { return (J + 1) * (J + 2) / 2; }
+inline int pairs_for(int J) { return (J + 1) * (J + 2) / 2 - 1; }
 
 }  // namespace
 }  // namespace gtk

@@ -117,8 +117,14 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
   const int lvl_stride = NPT * J * kThreads;
   const V *facn = reinterpret_cast<const V *>(a.fac[a.mode]);
   double err = 0;
+  GramAcc<V, gram_slots(J)> gram;
+  __syncthreads();
+  if (KIND == kUpdate) gram.init(s.pi, s.pj, a.E, tid & 31);
+  // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + TN - 1) / TN;
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+  const uint64_t tile_end = min(ntiles, (uint64_t)(blockIdx.x + 1) * per);
+  for (uint64_t tile = (uint64_t)blockIdx.x * per; tile < tile_end; ++tile) {
     __syncthreads();  // previous tile's reduction is done with the shared tile
     const uint64_t t0 = tile * TN;
     const int nv = (int)min((uint64_t)TN, a.nnz - t0);
@@ -179,7 +185,14 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
         s.rows[tl] = rowv[q];
       }
       __syncthreads();
-      gram_phase<V>(a, s, t0, nv, NPT);
+      if (a.dstore) {  // the tile's delta rows, contiguous in view order
+        V *dst = reinterpret_cast<V *>(a.dstore) + t0 * J;
+        for (int k = tid; k < nv * J; k += kThreads) dst[k] = s.dx[(k / J) * a.ldd + (k % J)];
+      }
+      // warp w reduces tile positions [w*TN/8, (w+1)*TN/8)
+      constexpr int R = TN / (kThreads / 32);
+      const int w0 = (tid >> 5) * R;
+      gram.run(s.dx, a.ldd, s.rows, w0, min(w0 + R, nv), a.gram, a.E, tid & 31);
     } else if (KIND == kFit) {
 #pragma unroll
       for (int q = 0; q < NPT; ++q) {
@@ -190,6 +203,7 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
       }
     }
   }
+  if (KIND == kUpdate) gram.flush(a.gram, a.E, tid & 31);
   if (KIND == kFit) {
     const double tot = block_sum(err);
     if (tid == 0) a.partial[blockIdx.x] = tot;
@@ -265,6 +279,10 @@ __global__ void __launch_bounds__(kThreads) k_mode_gen(ModeArgs a) {
       s.dx[tid * a.ldd + J] = x;
       s.rows[tid] = row;
       __syncthreads();
+      if (a.dstore) {
+        V *dst = reinterpret_cast<V *>(a.dstore) + t0 * J;
+        for (int k = tid; k < nv * J; k += kThreads) dst[k] = s.dx[(k / J) * a.ldd + (k % J)];
+      }
       gram_phase<V>(a, s, t0, nv, 1);
     } else if (KIND == kFit) {
       if (valid) {
@@ -280,13 +298,65 @@ __global__ void __launch_bounds__(kThreads) k_mode_gen(ModeArgs a) {
 }
 
 // ---------------------------------------------------------------- row solves
-// One warp per factor row: A = lambda I + Gram (FP64) in shared memory.
-// First Cholesky A = L L^T, L y = C, L^T a = y (A is symmetric positive definite
-// in exact arithmetic).  When rounding makes a pivot non-positive -- rows with
-// fewer nonzeros than J after ill-conditioned updates -- the row is solved again
-// by LU with partial pivoting, the method of the reference's Eigen inverse
-// (update.cuh:180), and bit 2 of *status counts it as a fallback (informational).
-// An exactly zero LU pivot sets bit 0 (GTK_ERR_NUMERIC); the row is still written.
+// A = lambda I + Gram (FP64), right-hand side C; a = A^-1 C overwrites the
+// factor row (cast to value_t), as update.cuh:163-194 does with Eigen's inverse.
+//
+// k_solve_rows: one thread per row.  The packed row (upper triangle + C, the
+// layout the Gram kernels accumulate) is copied to the thread's slice of shared
+// memory (element e of thread t at [e * blockDim + t], conflict-free) and
+// factored in place by upper Cholesky A = U^T U, then U^T y = C, U a = y.  GB300
+// issues FP64 at ~1/64 of FP32, so every lane works on its own row.  A row
+// whose pivot rounds to <= 0 (rows with fewer nonzeros than J after
+// ill-conditioned updates) is appended to a list and re-solved by
+// k_solve_lu_rows with LU and partial pivoting -- the method of the reference's
+// Eigen inverse (update.cuh:180) -- so the sweep never stops there either.
+
+__device__ __forceinline__ int upk(int i, int j, int J) {  // packed index of (i, j), i <= j <= J
+  return i * (J + 1) - (i * (i - 1)) / 2 + (j - i);
+}
+
+template <class V>
+__global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf,
+                             V *__restrict__ fac, double lambda, uint32_t *__restrict__ fallback,
+                             unsigned int *__restrict__ nfallback) {
+  extern __shared__ double sm[];
+  const int T = blockDim.x, tid = threadIdx.x;
+  double *A = sm + tid;  // element e at A[e * T]
+  for (uint64_t row = (uint64_t)blockIdx.x * T + tid; row < rows; row += (uint64_t)gridDim.x * T) {
+    const double *g = gram + row * (uint64_t)E;
+    for (int e = 0; e < E; ++e) A[e * T] = g[e];
+    for (int i = 0; i < J; ++i) A[upk(i, i, J) * T] += lambda;
+    bool ok = true;
+    for (int k = 0; k < J && ok; ++k) {
+      const double d = A[upk(k, k, J) * T];
+      if (!(d > 0.0) || !isfinite(d)) {
+        ok = false;
+        break;
+      }
+      const double u = sqrt(d), r = 1.0 / u;
+      A[upk(k, k, J) * T] = u;
+      for (int j = k + 1; j <= J; ++j) A[upk(k, j, J) * T] *= r;  // row k of U, and C_k / u_kk
+      for (int i = k + 1; i < J; ++i) {
+        const double uki = A[upk(k, i, J) * T];
+        for (int j = i; j <= J; ++j) A[upk(i, j, J) * T] -= uki * A[upk(k, j, J) * T];
+      }
+    }
+    // the elimination above also carried C through U^T y = C: column J now holds y
+    V *frow = fac + row * (uint64_t)ldf;
+    if (ok) {
+      for (int k = J - 1; k >= 0; --k) {
+        double v = A[upk(k, J, J) * T];
+        for (int j = k + 1; j < J; ++j) v -= A[upk(k, j, J) * T] * A[upk(j, J, J) * T];
+        v /= A[upk(k, k, J) * T];
+        A[upk(k, J, J) * T] = v;
+      }
+      for (int j = 0; j < ldf; ++j) frow[j] = j < J ? (V)A[upk(j, J, J) * T] : V(0);
+    } else {
+      fallback[atomicAdd(nfallback, 1u)] = (uint32_t)row;
+    }
+  }
+}
+
 // decode entry e of the packed row into (i, j), 0 <= i <= j <= J
 __device__ __forceinline__ void pair_of(int e, int J, int &i, int &j) {
   int off = 0;
@@ -300,13 +370,9 @@ __device__ __forceinline__ void pair_of(int e, int J, int &i, int &j) {
 
 __device__ void load_system(const double *__restrict__ g, int J, int E, double lambda, double *A, double *b,
                             int lane) {
-  for (int e = lane; e < E - 1; e += 32) {  // the last entry, sum x^2, is not part of the system
-    int i = 0, off = 0;
-    while (off + (J + 1 - i) <= e) {
-      off += J + 1 - i;
-      ++i;
-    }
-    const int j = i + (e - off);
+  for (int e = lane; e < E; e += 32) {
+    int i, j;
+    pair_of(e, J, i, j);
     const double v = g[e];
     if (j == J) {
       b[i] = v;
@@ -318,39 +384,6 @@ __device__ void load_system(const double *__restrict__ g, int J, int E, double l
   __syncwarp();
   for (int i = lane; i < J; i += 32) A[i * J + i] += lambda;
   __syncwarp();
-}
-
-// returns false when a pivot was not positive (A is left partly factored)
-__device__ bool cholesky_solve(double *A, double *b, int J, int lane) {
-  for (int k = 0; k < J; ++k) {
-    const double d = A[k * J + k];
-    if (!(d > 0.0) || !isfinite(d)) return false;  // uniform across the warp
-    const double lkk = sqrt(d);
-    __syncwarp();
-    for (int i = k + 1 + lane; i < J; i += 32) A[i * J + k] /= lkk;
-    if (lane == 0) A[k * J + k] = lkk;
-    __syncwarp();
-    for (int i = k + 1 + lane; i < J; i += 32) {
-      const double lik = A[i * J + k];
-      for (int j = k + 1; j <= i; ++j) A[i * J + j] -= lik * A[j * J + k];
-    }
-    __syncwarp();
-  }
-  for (int k = 0; k < J; ++k) {
-    const double yk = b[k] / A[k * J + k];
-    __syncwarp();
-    if (lane == 0) b[k] = yk;
-    for (int i = k + 1 + lane; i < J; i += 32) b[i] -= A[i * J + k] * yk;
-    __syncwarp();
-  }
-  for (int k = J - 1; k >= 0; --k) {
-    const double ak = b[k] / A[k * J + k];
-    __syncwarp();
-    if (lane == 0) b[k] = ak;
-    for (int i = lane; i < k; i += 32) b[i] -= A[k * J + i] * ak;
-    __syncwarp();
-  }
-  return true;
 }
 
 // LU with partial (row) pivoting, applied to b on the fly; returns false on an exactly zero pivot
@@ -412,59 +445,46 @@ __device__ bool lu_solve(double *A, double *b, int J, int lane) {
   return ok;
 }
 
+// one warp per listed row: LU with partial pivoting; sets bit 2 of *status
+// (informational) and bit 0 on an exactly zero pivot (GTK_ERR_NUMERIC)
 template <class V>
-__global__ void k_solve(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf, V *__restrict__ fac,
-                        int *__restrict__ status, double lambda, double *__restrict__ err_partial) {
+__global__ void k_solve_lu_rows(const double *__restrict__ gram, const uint32_t *__restrict__ list,
+                                const unsigned int *__restrict__ nlist, uint64_t all_rows, int J, int E, int ldf,
+                                V *__restrict__ fac, int *__restrict__ status, double lambda) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
   double *A = sm + (size_t)wib * ((size_t)J * J + J);
   double *b = A + (size_t)J * J;
-  double err = 0;  // sum over this warp's rows of sum_t (x_t - delta_t . a)^2
-  for (uint64_t row = (uint64_t)blockIdx.x * wpb + wib; row < rows; row += (uint64_t)gridDim.x * wpb) {
-    const double *g = gram + row * (uint64_t)E;
-    load_system(g, J, E, lambda, A, b, lane);
-    if (!cholesky_solve(A, b, J, lane)) {
-      __syncwarp();
-      load_system(g, J, E, lambda, A, b, lane);
-      const bool ok = lu_solve(A, b, J, lane);
-      if (lane == 0) atomicOr(status, ok ? 4 : 1);
-    }
-    V *frow = fac + row * (uint64_t)ldf;
+  const uint64_t n = list ? (uint64_t)*nlist : all_rows;  // list == nullptr: every row, in order
+  for (uint64_t k = (uint64_t)blockIdx.x * wpb + wib; k < n; k += (uint64_t)gridDim.x * wpb) {
+    const uint32_t row = list ? list[k] : (uint32_t)k;
+    load_system(gram + (uint64_t)row * E, J, E, lambda, A, b, lane);
+    const bool ok = lu_solve(A, b, J, lane);
+    if (lane == 0 && (list || !ok)) atomicOr(status, ok ? 4 : 1);
+    V *frow = fac + (uint64_t)row * ldf;
     for (int j = lane; j < ldf; j += 32) frow[j] = j < J ? (V)b[j] : V(0);
-    if (err_partial) {
-      // with the stored (value_t) row a: sum x^2 - 2 a.C + a^T G a, G = B - lambda I
-      __syncwarp();
-      double e_row = 0;
-      for (int e = lane; e < E; e += 32) {
-        int i, j;
-        pair_of(e, J, i, j);
-        const double v = g[e];
-        if (i == J) {
-          e_row += v;
-        } else {
-          const double ai = (double)(V)b[i];
-          if (j == J)
-            e_row -= 2.0 * ai * v;
-          else
-            e_row += (i == j ? 1.0 : 2.0) * ai * (double)(V)b[j] * v;
-        }
-      }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) e_row += __shfl_xor_sync(0xFFFFFFFFu, e_row, o);
-      err += e_row;
-    }
     __syncwarp();
   }
-  if (err_partial) {
-    __shared__ double werr[32];
-    if (lane == 0) werr[wib] = err;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double s = 0;
-      for (int w = 0; w < wpb; ++w) s += werr[w];
-      err_partial[blockIdx.x] = s;
-    }
+}
+
+// the fit from the delta of the last mode's pass (stored in view order):
+// x_hat = delta . a_{N-1}[i_{N-1}] in value_t (reconstruction.cuh:58-81 reduced to
+// one dot product), error (x - x_hat)^2 summed in FP64 per CTA
+template <class V>
+__global__ void k_fit_stored(const V *__restrict__ dstore, const uint32_t *__restrict__ row_of,
+                             const V *__restrict__ val, const V *__restrict__ fac, uint64_t nnz, int J, int ldf,
+                             double *__restrict__ partial) {
+  double err = 0;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nnz; t += (uint64_t)gridDim.x * blockDim.x) {
+    const V *d = dstore + t * (uint64_t)J;
+    const V *a = fac + (uint64_t)row_of[t] * ldf;
+    V xh = V(0);
+    for (int j = 0; j < J; ++j) xh += d[j] * a[j];
+    const V e = val[t] - xh;
+    err += (double)e * (double)e;
   }
+  const double tot = block_sum(err);
+  if (threadIdx.x == 0) partial[blockIdx.x] = tot;
 }
 
 __global__ void k_sum_fit(const double *__restrict__ partial, int m, double *__restrict__ out) {
@@ -513,6 +533,7 @@ template <class V, int KIND> bool find_spec(Launch &L, const DevTensor &t) {
 }
 
 constexpr size_t kSmemLimit = 227 * 1024;
+constexpr int kThreadSolveMaxJ = 24;  // larger ranks solve one row per warp
 
 template <class V, int KIND> int choose(Launch &L, const DevTensor &t, bool &gp_in_smem) {
   gp_in_smem = true;
@@ -615,7 +636,10 @@ template <class V, int KIND> static int launch_mode(DevTensor &t, int mode, void
   if (int rc = prepare_fn(L.fn, L.smem)) return rc;
   ModeArgs a = make_args(t, mode);
   a.gp_in_smem = gp_in_smem ? 1 : 0;
-  a.out = out;
+  if (KIND == kUpdate)
+    a.dstore = out;  // optional: delta of every nonzero, view order
+  else
+    a.out = out;
   int per_sm = 0;
   GTK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, kThreads, L.smem));
   if (per_sm < 1) return fail(GTK_ERR_UNSUPPORTED, "mode kernel does not fit on an SM");
@@ -631,37 +655,61 @@ template <class V, int KIND> static int launch_mode(DevTensor &t, int mode, void
 
 template <class V> static int update_impl(DevTensor &t, int mode) {
   const int E = pairs_for(t.J);
+  const int J = t.J;
+  const bool last = mode == t.N - 1;
+  // the last mode's pass also stores delta, from which the sweep's fit follows exactly
+  void *dstore = nullptr;
+  if (last && t.nnz) {
+    if (!t.dstore && !t.dstore_failed) {
+      if (dalloc(t, &t.dstore, t.nnz * (size_t)J * sizeof(V))) {
+        t.dstore = nullptr;
+        t.dstore_failed = true;  // no room: the fit recomputes delta instead
+        cudaGetLastError();
+      }
+    }
+    dstore = t.dstore;
+  }
+  t.fit_from_store = false;
   cudaEvent_t ev = nullptr;
   if (int rc = prof_begin(t, &ev)) return rc;
   GTK_CUDA(cudaMemsetAsync(t.gram, 0, t.rows[mode] * (uint64_t)E * 8, t.stream));
   if (t.nnz) {
     if (t.precision != GTK_PREC_PLAIN) {
-      if (int rc = run_mode_tc(t, mode, 0, nullptr, nullptr)) return rc;
-    } else if (int rc = launch_mode<V, kUpdate>(t, mode, nullptr, nullptr)) {
+      if (int rc = run_mode_tc(t, mode, 0, dstore, nullptr)) return rc;
+    } else if (int rc = launch_mode<V, kUpdate>(t, mode, dstore, nullptr)) {
       return rc;
     }
+    t.launches += 1;
   }
   if (int rc = prof_end(t, 0, ev)) return rc;
   if (int rc = prof_begin(t, &ev)) return rc;
-  const int J = t.J;
-  const size_t per_warp = ((size_t)J * J + J) * 8;
-  int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (48 * 1024) / per_warp));
-  const size_t smem = per_warp * wpb;
-  if (int rc = prepare_fn((const void *)k_solve<V>, smem)) return rc;
-  uint64_t grid = (t.rows[mode] + wpb - 1) / wpb;
-  grid = std::min<uint64_t>(grid, (uint64_t)t.num_sms * 32);
-  // the last mode's Gram rows also give the fit of the sweep: its delta is built
-  // from the modes already updated in this sweep, so sum_t (x_t - delta_t . a_new)^2
-  // = sum x^2 - 2 a.C + a^T G a per row (reconstruction.cuh:259-268 without a
-  // second J^N pass over the nonzeros)
-  const bool last = mode == t.N - 1;
-  if (last) grid = std::min<uint64_t>(grid, kFitGridMax);
-  if (grid < 1) grid = 1;
-  k_solve<V><<<(unsigned)grid, wpb * 32, smem, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf, (V *)t.fac[mode],
-                                                           t.status, kLambda, last ? t.partial : nullptr);
-  GTK_CUDA(cudaGetLastError());
-  t.fit_from_gram = last;
-  t.fit_grid = (int)grid;
+  GTK_CUDA(cudaMemsetAsync(t.nfallback, 0, 4, t.stream));
+  const size_t lu_warp = ((size_t)J * J + J) * 8;
+  const int lu_wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (48 * 1024) / lu_warp));
+  const size_t lu_smem = lu_warp * lu_wpb;
+  if (int rc = prepare_fn((const void *)k_solve_lu_rows<V>, lu_smem)) return rc;
+  if (J <= kThreadSolveMaxJ) {
+    const int T = J <= 12 ? 128 : 64;
+    const size_t smem = (size_t)T * E * 8;
+    if (int rc = prepare_fn((const void *)k_solve_rows<V>, smem)) return rc;
+    uint64_t grid = (t.rows[mode] + T - 1) / T;
+    if (grid < 1) grid = 1;
+    k_solve_rows<V><<<(unsigned)grid, T, smem, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf, (V *)t.fac[mode],
+                                                           kLambda, t.fallback, t.nfallback);
+    GTK_CUDA(cudaGetLastError());
+    k_solve_lu_rows<V><<<(unsigned)t.num_sms, lu_wpb * 32, lu_smem, t.stream>>>(
+        t.gram, t.fallback, t.nfallback, 0, J, E, t.ldf, (V *)t.fac[mode], t.status, kLambda);
+    GTK_CUDA(cudaGetLastError());
+    t.launches += 2;
+  } else {
+    uint64_t grid = std::min<uint64_t>((t.rows[mode] + lu_wpb - 1) / lu_wpb, (uint64_t)t.num_sms * 32);
+    if (grid < 1) grid = 1;
+    k_solve_lu_rows<V><<<(unsigned)grid, lu_wpb * 32, lu_smem, t.stream>>>(
+        t.gram, nullptr, t.nfallback, t.rows[mode], J, E, t.ldf, (V *)t.fac[mode], t.status, kLambda);
+    GTK_CUDA(cudaGetLastError());
+    t.launches += 1;
+  }
+  t.fit_from_store = dstore != nullptr;
   if (int rc = prof_end(t, 1, ev)) return rc;
   return 0;
 }
@@ -674,9 +722,14 @@ template <class V> static int fit_impl(DevTensor &t, double *fit) {
   cudaEvent_t ev = nullptr;
   if (int rc = prof_begin(t, &ev)) return rc;
   int grid = 1;
-  if (t.fit_from_gram) {
-    grid = t.fit_grid;  // the error partials of the last mode's solve
+  if (t.fit_from_store && t.nnz) {
+    grid = (int)std::min<uint64_t>(kFitGridMax, (t.nnz + 255) / 256);
+    k_fit_stored<V><<<grid, 256, 0, t.stream>>>((const V *)t.dstore, t.vidx[t.N - 1][t.N - 1], (const V *)t.vval[t.N - 1],
+                                                (const V *)t.fac[t.N - 1], t.nnz, t.J, t.ldf, t.partial);
+    GTK_CUDA(cudaGetLastError());
+    t.launches += 1;
   } else if (t.nnz) {
+    t.launches += 1;
     if (t.precision != GTK_PREC_PLAIN) {
       if (int rc = run_mode_tc(t, t.N - 1, 1, nullptr, &grid)) return rc;
     } else if (int rc = launch_mode<V, kFit>(t, t.N - 1, nullptr, &grid)) {
@@ -687,11 +740,11 @@ template <class V> static int fit_impl(DevTensor &t, double *fit) {
   }
   k_sum_fit<<<1, 32, 0, t.stream>>>(t.partial, grid, t.partial + kFitGridMax);
   GTK_CUDA(cudaGetLastError());
+  t.launches += 1;
   if (int rc = prof_end(t, 2, ev)) return rc;
   double err = 0;
   GTK_CUDA(cudaMemcpyAsync(&err, t.partial + kFitGridMax, 8, cudaMemcpyDeviceToHost, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
-  if (err < 0) err = 0;  // the Gram form can round below zero at a perfect fit
   *fit = (t.norm == 0) ? 1.0 : 1.0 - std::sqrt(err) / t.norm;
   return 0;
 }

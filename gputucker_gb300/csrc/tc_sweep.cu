@@ -150,7 +150,7 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int A_BYTES = kTcThreads * KP * ES;
   static constexpr int B_BYTES = NP * KP * ES;
   static constexpr int LDD = ((J + 1) & 1) ? J + 1 : J + 2;
-  static constexpr int E = (J + 1) * (J + 2) / 2;
+  static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
   static constexpr int OFF_B = A_BYTES;
   static constexpr int OFF_DX = (OFF_B + B_BYTES + 15) / 16 * 16;
   static constexpr int OFF_ROWS = OFF_DX + (kTcThreads * LDD * 4 + 15) / 16 * 16;
@@ -217,37 +217,57 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   double err = 0;
   uint32_t phase = 0;
   bool timed_out = false;
+  GramAcc<float, gram_slots(J)> gram;
+  if (KIND == 0) gram.init(ts.pi, ts.pj, S::E, tid & 31);
+  // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
-  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+  const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
+  const uint64_t tile_end = min(ntiles, (uint64_t)(blockIdx.x + 1) * per);
+  // inputs of one tile for this thread: its nonzero's row, value and the factor
+  // rows (p, q form the Kronecker operand; e1 (D = 3) finishes the contraction)
+  struct TileIn {
+    uint32_t row;
+    float x;
+    float p[LDG], q[LDG], e1[LDG];
+  };
+  auto load_tile = [&](uint64_t tl, TileIn &in) {
+    const uint64_t b0 = tl * kTcThreads;
+    const int n_valid = (int)min((uint64_t)kTcThreads, a.nnz - b0);
+    const bool ok = tid < n_valid;
+    const uint64_t g = ok ? b0 + tid : b0;
+    in.row = ok ? a.coord[a.mode][g] : 0xFFFFFFFFu;
+    in.x = ok ? reinterpret_cast<const float *>(a.val)[g] : 0.f;
+    const float4 *fp = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 2]]) +
+                                                        (size_t)a.coord[a.others[D - 2]][g] * LDG);
+    const float4 *fq = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 1]]) +
+                                                        (size_t)a.coord[a.others[D - 1]][g] * LDG);
+#pragma unroll
+    for (int c = 0; c < LDG / 4; ++c) {
+      const float4 u = __ldg(fp + c), w = __ldg(fq + c);
+      in.p[4 * c] = u.x, in.p[4 * c + 1] = u.y, in.p[4 * c + 2] = u.z, in.p[4 * c + 3] = u.w;
+      in.q[4 * c] = w.x, in.q[4 * c + 1] = w.y, in.q[4 * c + 2] = w.z, in.q[4 * c + 3] = w.w;
+    }
+    if (D == 3) {
+      const float4 *fe = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[0]]) +
+                                                          (size_t)a.coord[a.others[0]][g] * LDG);
+#pragma unroll
+      for (int c = 0; c < LDG / 4; ++c) {
+        const float4 u = __ldg(fe + c);
+        in.e1[4 * c] = u.x, in.e1[4 * c + 1] = u.y, in.e1[4 * c + 2] = u.z, in.e1[4 * c + 3] = u.w;
+      }
+    }
+  };
+  TileIn cur;
+  const uint64_t tile_begin = (uint64_t)blockIdx.x * per;
+  if (tile_begin < tile_end) load_tile(tile_begin, cur);
+  for (uint64_t tile = tile_begin; tile < tile_end; ++tile) {
     const uint64_t t0 = tile * kTcThreads;
     const int nv = (int)min((uint64_t)kTcThreads, a.nnz - t0);
     const bool valid = tid < nv;
     const uint64_t gi = valid ? t0 + tid : t0;
-    const uint32_t row = valid ? a.coord[a.mode][gi] : 0xFFFFFFFFu;
-    const float x = valid ? reinterpret_cast<const float *>(a.val)[gi] : 0.f;
-    // factor rows: p, q form the Kronecker operand; e (D = 3) finishes the contraction
-    float p[LDG], q[LDG], e1[LDG];
-    {
-      const float4 *fp = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 2]]) +
-                                                          (size_t)a.coord[a.others[D - 2]][gi] * LDG);
-      const float4 *fq = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 1]]) +
-                                                          (size_t)a.coord[a.others[D - 1]][gi] * LDG);
-#pragma unroll
-      for (int c = 0; c < LDG / 4; ++c) {
-        const float4 u = __ldg(fp + c), w = __ldg(fq + c);
-        p[4 * c] = u.x, p[4 * c + 1] = u.y, p[4 * c + 2] = u.z, p[4 * c + 3] = u.w;
-        q[4 * c] = w.x, q[4 * c + 1] = w.y, q[4 * c + 2] = w.z, q[4 * c + 3] = w.w;
-      }
-      if (D == 3) {
-        const float4 *fe = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[0]]) +
-                                                            (size_t)a.coord[a.others[0]][gi] * LDG);
-#pragma unroll
-        for (int c = 0; c < LDG / 4; ++c) {
-          const float4 u = __ldg(fe + c);
-          e1[4 * c] = u.x, e1[4 * c + 1] = u.y, e1[4 * c + 2] = u.z, e1[4 * c + 3] = u.w;
-        }
-      }
-    }
+    const uint32_t row = cur.row;
+    const float x = cur.x;
+    const float *p = cur.p, *q = cur.q;
     // A row `tid`: the Kronecker product p (x) q, rounded to the MMA input type
 #pragma unroll
     for (int c = 0; c < S::KP / S::EPC; ++c) {
@@ -270,6 +290,9 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
                   s > 0 ? 1u : 0u);
       mma_commit(bar);
     }
+    // the next tile's loads overlap this tile's MMAs, epilogue and reduction
+    TileIn nxt;
+    if (tile + 1 < tile_end) load_tile(tile + 1, nxt);
     uint32_t spins = 0;
     bool done = false;
     while (!(done = mbar_try_wait(bar, phase)) && ++spins < kWaitLimit) {
@@ -297,7 +320,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
           if (D == 2)
             delta[col] = v[i];
           else
-            delta[col / J] += e1[col % J] * v[i];
+            delta[col / J] += cur.e1[col % J] * v[i];
         }
       }
     }
@@ -308,7 +331,11 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
       ts.dx[tid * S::LDD + J] = x;
       ts.rows[tid] = row;
       __syncthreads();
-      gram_phase<float>(a, ts, t0, nv, 1);
+      if (a.dstore) {  // the tile's delta rows, contiguous in view order
+        float *dst = reinterpret_cast<float *>(a.dstore) + t0 * J;
+        for (int k = tid; k < nv * J; k += kTcThreads) dst[k] = ts.dx[(k / J) * S::LDD + (k % J)];
+      }
+      gram.run(ts.dx, S::LDD, ts.rows, warp * 32, min(warp * 32 + 32, nv), a.gram, S::E, tid & 31);
       __syncthreads();
     } else if (KIND == 1) {
       if (valid) {
@@ -327,7 +354,9 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
       }
       __syncthreads();
     }
+    cur = nxt;
   }
+  if (KIND == 0) gram.flush(a.gram, S::E, tid & 31);
   if (KIND == 1) {
     const double tot = block_sum(err);
     if (tid == 0) a.partial[blockIdx.x] = tot;
@@ -379,8 +408,16 @@ int tc_prepare(const TcLaunch &L, int num_sms, int *grid_cap, int *smem_out) {
   int smem = L.smem;
   if ((smem + 1024) * (max_ctas + 1) <= sm_bytes) smem = sm_bytes / (max_ctas + 1) - 1024 + 16;
   GTK_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
-  int per_sm = 0;
-  GTK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, kTcThreads, smem));
+  GTK_CUDA(cudaFuncSetAttribute(L.fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  cudaFuncAttributes fa;
+  GTK_CUDA(cudaFuncGetAttributes(&fa, L.fn));
+  // residency from the kernel's own limits (shared memory incl. the 1 KB the
+  // driver reserves per CTA, registers, threads); the occupancy API has been
+  // seen to under-report it for this kernel
+  int per_sm = sm_bytes / (smem + (int)fa.sharedSizeBytes + 1024);
+  const int regs = fa.numRegs > 0 ? fa.numRegs : 64;
+  per_sm = std::min(per_sm, 65536 / (regs * kTcThreads));
+  per_sm = std::min(per_sm, 2048 / kTcThreads);
   if (per_sm < 1) return fail(GTK_ERR_UNSUPPORTED, "tensor-core mode kernel does not fit on an SM");
   if (per_sm > max_ctas) return fail(GTK_ERR_UNSUPPORTED, "tensor-core kernel would oversubscribe TMEM");
   *grid_cap = per_sm * num_sms;
@@ -413,7 +450,10 @@ int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   a.val = t.vval[mode];
   a.corep = t.corep[mode];
   a.vperm = t.vperm[mode];
-  a.out = out;
+  if (kind == 0)
+    a.dstore = out;
+  else
+    a.out = out;
   a.gram = t.gram;
   a.partial = t.partial;
   a.status = t.status;

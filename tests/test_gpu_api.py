@@ -1,0 +1,153 @@
+"""The public API end to end on the GPU: files -> decomposition, the CLI, errors."""
+
+import glob
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import gputucker_gb300 as gtk
+from gputucker_gb300 import _native as nat
+from oracle_util import ROOT, Oracle, random_coo, rel_fro, write_tns
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = sorted(glob.glob(os.path.join(ROOT, "tests", "golden", "*.npz")))
+
+
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
+def test_golden_through_public_api(path):
+    """Reference-produced fixtures: parse -> blocks -> init (continuing the parser's
+    rand() stream) -> 3 sweeps, through the C ABI."""
+    g = np.load(path)
+    dtype = int(g["dtype"])
+    N = len(g["dims"])
+    P = [int(x) for x in g["P"]]
+    J = int(g["J"])
+    coo = gtk.parse_from_file(path[:-4] + ".tns", N, dtype, rand_seed=1)
+    assert coo.rand_draws == int(g["skip"])
+    with gtk.create_tensor_blocks(coo, P, J) as t:
+        for b in range(t.info.block_count):
+            coord, idx, vals = t.block(b)
+            s, e = int(g["blk_ptr"][b]), int(g["blk_ptr"][b + 1])
+            assert coord == [int(x) for x in g["blk_coord"][b]]
+            for n in range(N):
+                np.testing.assert_array_equal(idx[n], g[f"idx{n}"][s:e])
+                cnt, where = t.segments(b, n)
+                rows = t.info.block_dims[n] + 1
+                np.testing.assert_array_equal(cnt, g[f"count{n}"][b * rows:(b + 1) * rows])
+                np.testing.assert_array_equal(where, g[f"where{n}"][s:e])
+            np.testing.assert_array_equal(vals, g["vals"][s:e])
+        t.init_random(1, coo.rand_draws)
+        for n in range(N):
+            np.testing.assert_array_equal(t.get_factor(n), g[f"fac0_{n}"])
+        np.testing.assert_array_equal(t.get_core(), g["core"])
+        for s in range(3):
+            t.update_factor_matrices()
+            fit = t.reconstruction()
+            if dtype == 1:
+                for n in range(N):
+                    assert rel_fro(t.get_factor(n), g[f"fac{s + 1}_{n}"]) <= 1e-9
+                # the reference sums the error in value_t serially; the fixtures are FP64 here
+                assert abs(fit - float(g[f"fit{s + 1}"])) <= 1e-9
+            else:
+                # FP32: the reference's fit sums the error in float; within its rounding
+                assert abs(fit - float(g[f"fit{s + 1}"])) <= 1e-4
+
+
+def test_cli_end_to_end(tmp_path):
+    from gputucker_gb300 import build
+    rng = np.random.default_rng(5)
+    dims = [30, 40, 35]
+    idx = random_coo(rng, dims, 6000)
+    vals = rng.random(len(idx[0]))
+    f = tmp_path / "t.tns"
+    write_tns(f, idx, vals, dtype=1)
+    r = subprocess.run([build.CLI, "-i", str(f), "-o", "3", "-r", "6", "-p", "2,2,1", "--iters", "3",
+                        "--write-factors", str(tmp_path / "A")], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    fits = [float(x) for x in re.findall(r"^iter \d+\t Fit: (\S+)$", r.stdout, flags=re.M)]
+    ora = Oracle(1, idx, vals, dims, [2, 2, 1], 6)
+    ora.init_random(1, 0)
+    ofits = []
+    for it in range(3):
+        ofits.append(ora.sweep()["fit64"])
+        if it > 0 and abs(ofits[-1] - ofits[-2]) <= 1e-4:
+            break
+    assert len(fits) == len(ofits)
+    np.testing.assert_allclose(fits, ofits, atol=1e-9)
+    a0 = np.loadtxt(tmp_path / "A0.txt")
+    assert rel_fro(a0, ora.get_factor(0)[:dims[0]]) <= 1e-9
+
+
+def test_state_error_before_init():
+    coo = gtk.coo_from_arrays([np.arange(10, dtype=np.uint32)] * 3, np.ones(10))
+    with gtk.create_tensor_blocks(coo, [1, 1, 1], 4) as t:
+        with pytest.raises(gtk.GTKError) as e:
+            t.update_factor_matrices()
+        assert e.value.code == nat.GTK_ERR_STATE
+        with pytest.raises(gtk.GTKError) as e:
+            t.update_mode(3)
+        assert e.value.code in (nat.GTK_ERR_STATE, nat.GTK_ERR_ARG)
+
+
+def test_memory_cap_reports_oom(monkeypatch):
+    """An allocation cap (GTK_DEVICE_MEMORY_CAP) stands in for an exhausted HBM."""
+    coo = gtk.generate(3, [1000] * 3, 100_000, "uniform", 0, "uniform", "f32", seed=1)
+    monkeypatch.setenv("GTK_DEVICE_MEMORY_CAP", str(1 << 20))
+    with pytest.raises(gtk.GTKError) as e:
+        gtk.create_tensor_blocks(coo, [1, 1, 1], 8)
+    assert e.value.code == nat.GTK_ERR_OOM
+    monkeypatch.delenv("GTK_DEVICE_MEMORY_CAP")
+    with gtk.create_tensor_blocks(coo, [1, 1, 1], 8) as t:
+        assert t.info.device_bytes > (1 << 20)
+
+
+def test_direct_fit_after_set_factor_matches_gram_fit():
+    """The fit from the last mode's Gram rows equals the direct reconstruction."""
+    rng = np.random.default_rng(2)
+    dims = [25, 30, 20, 22]
+    idx = random_coo(rng, dims, 8000)
+    vals = rng.random(len(idx[0]))
+    coo = gtk.coo_from_arrays(idx, vals, dims=dims)
+    with gtk.create_tensor_blocks(coo, [2, 1, 2, 1], 6) as t:
+        t.init_random(1, 0)
+        t.update_factor_matrices()
+        f_gram = t.reconstruction()
+        t.set_factor(0, t.get_factor(0))  # invalidates the Gram-derived fit
+        f_direct = t.reconstruction()
+        assert abs(f_gram - f_direct) <= 1e-10
+
+
+def test_profile_and_timer():
+    coo = gtk.generate(3, [500] * 3, 50_000, "zipf", 1.1, "uniform", "f32", seed=4)
+    with gtk.create_tensor_blocks(coo, [1, 1, 1], 8) as t:
+        t.init_random(1, 0)
+        t.profile(True)
+        t.timer_begin()
+        t.update_factor_matrices()
+        t.reconstruction()
+        ms = t.timer_end()
+        k_ms, k_n = t.profile_read(0)
+        s_ms, s_n = t.profile_read(1)
+        assert k_n == 3 and s_n == 3 and 0 < k_ms <= ms * 1.5 and ms > 0
+        t.profile_reset()
+        assert t.profile_read(3) == (0.0, 0)
+
+
+def test_compute_delta_block_major_order():
+    """gtk_compute_delta returns delta in the reference's block-major order."""
+    rng = np.random.default_rng(9)
+    dims = [20, 21, 22]
+    idx = random_coo(rng, dims, 3000)
+    vals = rng.random(len(idx[0]))
+    coo = gtk.coo_from_arrays(idx, vals, dims=dims)
+    P = [2, 3, 2]
+    with gtk.create_tensor_blocks(coo, P, 5) as t:
+        ora = Oracle(1, idx, vals, dims, P, 5)
+        t.init_random(1, 0)
+        ora.init_random(1, 0)
+        for n in range(3):
+            assert rel_fro(t.compute_delta(n), ora.delta(n)) <= 1e-13
