@@ -93,6 +93,8 @@ SIGNATURES = {
     "gtk_reconstruction": (C.c_int, [P, C.POINTER(C.c_double)]),
     "gtk_tucker_decomposition": (C.c_int, [P, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "gtk_compute_delta": (C.c_int, [P, C.c_int, P]),
+    "gtk_sweep": (C.c_int, [P, C.POINTER(C.c_double)]),
+    "gtk_set_graph": (C.c_int, [P, C.c_int]),
     "gtk_generate": (C.c_int, [C.c_int, U32P, C.c_uint64, C.c_int, C.c_double, C.c_int, C.c_int, C.c_uint64,
                                C.POINTER(P)]),
     "gtk_generate_planted": (C.c_int, [C.c_int, U32P, C.c_uint64, C.c_int, C.c_double, C.c_int, C.c_uint64,

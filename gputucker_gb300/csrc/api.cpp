@@ -60,6 +60,7 @@ int dalloc(DevTensor &t, void **p, size_t bytes) {
 static void release(DevTensor &t) {
   if (t.dev >= 0) cudaSetDevice(t.dev);
   if (t.stream) cudaStreamSynchronize(t.stream);
+  drop_graph(t);
   for (void *p : t.allocs) cudaFree(p);
   t.allocs.clear();
   if (t.tev0) cudaEventDestroy(t.tev0);
@@ -309,6 +310,7 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
   A((void **)&t->partial, kPartialDoubles * 8);
   A((void **)&t->status, 16);
   A((void **)&t->fallback, max_rows * 4);
+  A((void **)&t->fallback64, max_rows * 4);
   A((void **)&t->nfallback, 16);
   if (rc) return bail(rc);
   for (int n = 0; n < N; ++n) {
@@ -467,6 +469,7 @@ int gtk_set_precision(gtk_tensor *t, int precision) {
   if (precision != GTK_PREC_PLAIN && precision != GTK_PREC_BF16 && precision != GTK_PREC_TF32)
     return fail(GTK_ERR_ARG, "unknown precision");
   t->fit_from_store = false;
+  drop_graph(*t);
   if (precision != GTK_PREC_PLAIN && !tc_supported(t->N, t->J, t->dtype))
     return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this order/rank/value type (FP32, N = 3 or 4, "
                                      "J in {4, 8, 10, 12, 16} for N = 3 and {4, 8, 10, 12} for N = 4)");
@@ -497,6 +500,23 @@ int gtk_update_factor_matrices(gtk_tensor *t) {
   GTK_GUARD_END
 }
 
+int gtk_sweep(gtk_tensor *t, double *fit) {
+  if (int rc = ready(t)) return rc;
+  if (!fit) return fail(GTK_ERR_ARG, "null fit");
+  GTK_GUARD_BEGIN
+  if (int rc = run_sweep(*t, fit)) return rc;
+  return check_status(*t);
+  GTK_GUARD_END
+}
+
+int gtk_set_graph(gtk_tensor *t, int on) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (int rc = set_dev(t)) return rc;
+  t->use_graph = on != 0;
+  if (!t->use_graph) drop_graph(*t);
+  return 0;
+}
+
 int gtk_reconstruction(gtk_tensor *t, double *fit) {
   if (int rc = ready(t)) return rc;
   if (!fit) return fail(GTK_ERR_ARG, "null fit");
@@ -515,9 +535,7 @@ int gtk_tucker_decomposition(gtk_tensor *t, int max_iters, double tol, double *f
   double p_fit = -1, fit = -1;
   int numeric = 0;
   while (true) {
-    for (int n = 0; n < t->N; ++n)
-      if (int rc = run_update_mode(*t, n)) return rc;
-    if (int rc = run_fit(*t, &fit)) return rc;
+    if (int rc = run_sweep(*t, &fit)) return rc;
     if (check_status(*t)) numeric = GTK_ERR_NUMERIC;
     if (fits) fits[it] = fit;
     ++it;

@@ -127,8 +127,13 @@ struct DevTensor {
   bool dstore_failed = false;
   void *dstore = nullptr;       // [nnz][J] value_t, view order of the last mode
   uint32_t *fallback = nullptr; // rows re-solved by pivoted LU
+  uint32_t *fallback64 = nullptr; // precision form: rows re-solved in FP64
   unsigned int *nfallback = nullptr;
-  uint64_t launches = 0;        // kernels launched by the sweep entry points  // sweeps in which some row needed the pivoted-LU fallback
+  uint64_t launches = 0;        // kernels launched by the sweep entry points
+  bool use_graph = false;       // gtk_sweep replays a captured CUDA graph
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  uint64_t graph_kernels = 0;  // sweeps in which some row needed the pivoted-LU fallback
 
   // profiling
   bool prof = false;
@@ -151,6 +156,9 @@ int upload_core_perms(DevTensor &t, const void *core_host);
 int run_update_mode(DevTensor &t, int mode);
 int run_fit(DevTensor &t, double *fit);
 int run_delta(DevTensor &t, int mode, void *d_delta_blockmajor);
+int run_sweep(DevTensor &t, double *fit);
+int ensure_dstore(DevTensor &t);
+void drop_graph(DevTensor &t);
 // tc_sweep.cu: the tensor-core (BF16 / TF32) form; kind 0 update, 1 fit, 2 delta
 bool tc_supported(int N, int J, int dtype);
 int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used);

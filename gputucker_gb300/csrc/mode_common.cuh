@@ -201,46 +201,106 @@ __device__ void gram_phase(const ModeArgs &a, const TileSmem<V> &s, uint64_t til
 
 // Running Gram/RHS sums of one warp.  Lane l owns the entries e = l + 32k
 // (k < KE) of the packed row; the warp walks its slice of each tile in view
-// order, adding delta_i * delta_j (rounded to value_t) for every entry, and
-// flushes its sums with FP64 atomics whenever the row changes and at the end
-// of the CTA's (contiguous) range of tiles.  A long row thus costs one flush
-// per warp and CTA, a short row one or two flushes; no block-wide barrier is
-// needed inside the reduction.
-template <class V, int KE> struct GramAcc {
+// order, adding delta_i * delta_j for every entry, and flushes its sums with
+// FP64 atomics whenever the row changes and at the end of the CTA's
+// (contiguous) range of tiles.  A long row thus costs one flush per warp and
+// CTA, a short row one or two flushes; no block-wide barrier is needed.
+//   EXACT (the plain form): every product rounded to value_t as ComputingBC
+//     forms it (update.cuh:85-90) and added with Neumaier compensation.
+//   !EXACT (the tensor-core forms, whose delta carries BF16/TF32 rounding):
+//     plain FP32 fused multiply-adds within a tile slice (<= 64 terms), merged
+//     into the compensated running sum once per slice or row change.
+// Slots past the last entry read column zc of the tile (kept at zero), so the
+// inner loop has no branches.
+template <class V, int KE, bool EXACT> struct GramAcc {
   ProdSum<V> acc[KE];
+  V part[KE];
   int ei[KE], ej[KE];
   uint32_t row = 0xFFFFFFFFu;
 
-  __device__ void init(const unsigned char *pi, const unsigned char *pj, int E, int lane) {
+  __device__ void init(const unsigned char *pi, const unsigned char *pj, int E, int zc, int lane) {
 #pragma unroll
     for (int k = 0; k < KE; ++k) {
       const int e = lane + 32 * k;
-      ei[k] = e < E ? pi[e] : -1;
-      ej[k] = e < E ? pj[e] : 0;
+      ei[k] = e < E ? pi[e] : zc;
+      ej[k] = e < E ? pj[e] : zc;
       acc[k] = ProdSum<V>();
+      part[k] = V(0);
+    }
+  }
+  __device__ void merge() {
+    if (!EXACT) {
+#pragma unroll
+      for (int k = 0; k < KE; ++k) {
+        acc[k].add(part[k]);
+        part[k] = V(0);
+      }
     }
   }
   __device__ void flush(double *gram, int E, int lane) {
+    merge();
     if (row != 0xFFFFFFFFu) {
 #pragma unroll
       for (int k = 0; k < KE; ++k)
-        if (ei[k] >= 0) atomicAdd(gram + (size_t)row * E + lane + 32 * k, acc[k].value());
+        if (lane + 32 * k < E) atomicAdd(gram + (size_t)row * E + lane + 32 * k, acc[k].value());
     }
 #pragma unroll
     for (int k = 0; k < KE; ++k) acc[k] = ProdSum<V>();
   }
   // tile positions [t0, t1) of the shared delta tile (row stride ldd, column J = x)
   __device__ void run(const V *dx, int ldd, const uint32_t *rows, int t0, int t1, double *gram, int E, int lane) {
-    for (int t = t0; t < t1; ++t) {
-      const uint32_t r = rows[t];
-      if (r != row) {
-        flush(gram, E, lane);
-        row = r;
-      }
-      const V *d = dx + t * ldd;
+    if (EXACT) {
+      for (int t = t0; t < t1; ++t) {
+        const uint32_t r = rows[t];
+        if (r != row) {
+          flush(gram, E, lane);
+          row = r;
+        }
+        const V *d = dx + t * ldd;
 #pragma unroll
-      for (int k = 0; k < KE; ++k)
-        if (ei[k] >= 0) acc[k].add(mul_rn(d[ei[k]], d[ej[k]]));
+        for (int k = 0; k < KE; ++k) acc[k].add(mul_rn(d[ei[k]], d[ej[k]]));
+      }
+      return;
+    }
+    // runs of equal rows, 32 positions at a time: one ballot finds where rows change
+    for (int base = t0; base < t1; base += 32) {
+      const int n = min(32, t1 - base);
+      const uint32_t my = lane < n ? rows[base + lane] : 0xFFFFFFFFu;
+      const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, my, 1);
+      const bool head = lane < n && (lane == 0 ? my != row : my != prev);
+      uint32_t heads = __ballot_sync(0xFFFFFFFFu, head);
+      int a = 0;
+      while (a < n) {
+        if (heads & 1u) {  // a new row starts at position base + a
+          flush(gram, E, lane);
+          row = __shfl_sync(0xFFFFFFFFu, my, a);
+        }
+        // run [a, b): up to the next head
+        const uint32_t rest = heads >> 1;
+        const int b = rest ? min(n, a + 1 + __ffs(rest) - 1) : n;
+        V p4[KE][4];
+#pragma unroll
+        for (int k = 0; k < KE; ++k) p4[k][0] = p4[k][1] = p4[k][2] = p4[k][3] = V(0);
+        int t = base + a;
+        const int te = base + b;
+        for (; t + 4 <= te; t += 4) {
+          const V *d = dx + t * ldd;
+#pragma unroll
+          for (int u = 0; u < 4; ++u)
+#pragma unroll
+            for (int k = 0; k < KE; ++k) p4[k][u] = fma(d[u * ldd + ei[k]], d[u * ldd + ej[k]], p4[k][u]);
+        }
+        for (; t < te; ++t) {
+          const V *d = dx + t * ldd;
+#pragma unroll
+          for (int k = 0; k < KE; ++k) p4[k][0] = fma(d[ei[k]], d[ej[k]], p4[k][0]);
+        }
+#pragma unroll
+        for (int k = 0; k < KE; ++k) part[k] += (p4[k][0] + p4[k][1]) + (p4[k][2] + p4[k][3]);
+        merge();
+        heads = b - a >= 32 ? 0u : (heads >> (b - a));
+        a = b;
+      }
     }
   }
 };
@@ -262,7 +322,8 @@ __device__ inline double block_sum(double v) {
 }
 
 
-inline int ldd_for(int J) { return ((J + 1) & 1) ? J + 1 : J + 2; }
+// odd stride (conflict-free column writes) with a spare zero column at J + 1
+inline int ldd_for(int J) { return ((J + 2) & 1) ? J + 2 : J + 3; }
 inline int pairs_for(int J) { return (J + 1) * (J + 2) / 2 - 1; }
 
 }  // namespace

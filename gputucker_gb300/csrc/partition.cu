@@ -35,6 +35,7 @@ constexpr int kRsTile = kRsThreads * kRsRounds;
 constexpr int kScanThreads = 256;
 constexpr int kScanItems = 16;
 constexpr int kScanChunk = kScanThreads * kScanItems;
+constexpr uint32_t kHistSmemKeys = 8192;  // block histograms up to this many blocks count in shared memory
 
 struct Ptrs {
   const uint32_t *p[kMaxOrder];
@@ -238,9 +239,25 @@ __global__ void k_block_id(Ptrs g, int N, Dims dm, uint64_t n, uint32_t *__restr
   }
 }
 
-__global__ void k_count_u64(const uint32_t *__restrict__ key, uint64_t n, uint64_t *__restrict__ cnt) {
-  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
-    atomicAdd((unsigned long long *)&cnt[key[t]], 1ull);
+// histogram of keys < nkeys into cnt (u64); per-CTA shared counters when they fit
+__global__ void k_count_u64(const uint32_t *__restrict__ key, uint64_t n, uint64_t *__restrict__ cnt, uint32_t nkeys) {
+  extern __shared__ unsigned int hs[];
+  const bool local = nkeys <= kHistSmemKeys;
+  if (local) {
+    for (uint32_t k = threadIdx.x; k < nkeys; k += blockDim.x) hs[k] = 0;
+    __syncthreads();
+  }
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+    if (local)
+      atomicAdd(&hs[key[t]], 1u);
+    else
+      atomicAdd((unsigned long long *)&cnt[key[t]], 1ull);
+  }
+  if (local) {
+    __syncthreads();
+    for (uint32_t k = threadIdx.x; k < nkeys; k += blockDim.x)
+      if (hs[k]) atomicAdd((unsigned long long *)&cnt[k], (unsigned long long)hs[k]);
+  }
 }
 
 // gather the coordinates into block-major order; global copy gblk and local blk_idx
@@ -406,7 +423,10 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
   TRY(radix_sort(sbid, perm, n, bits_for(t.nblk - 1), sc, s));
   // blk_ptr
   TRY(ck(cudaMemsetAsync(t.blk_ptr, 0, (t.nblk + 1) * 8, s), "memset"));
-  if (n) k_count_u64<<<G, T, 0, s>>>(sbid, n, t.blk_ptr);
+  if (n) {
+    const size_t hsm = t.nblk <= kHistSmemKeys ? t.nblk * 4 : 0;
+    k_count_u64<<<G, T, hsm, s>>>(sbid, n, t.blk_ptr, (uint32_t)t.nblk);
+  }
   TRY(exclusive_scan<unsigned long long>((unsigned long long *)t.blk_ptr, t.nblk + 1, (unsigned long long *)sc.sums, s));
   // block-major arrays (global copy in gblk for the views)
   MPtrs gblk, lidx;

@@ -117,9 +117,10 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
   const int lvl_stride = NPT * J * kThreads;
   const V *facn = reinterpret_cast<const V *>(a.fac[a.mode]);
   double err = 0;
-  GramAcc<V, gram_slots(J)> gram;
+  GramAcc<V, gram_slots(J), true> gram;
+  for (int k = tid; k < TN; k += kThreads) s.dx[k * a.ldd + J + 1] = V(0);
   __syncthreads();
-  if (KIND == kUpdate) gram.init(s.pi, s.pj, a.E, tid & 31);
+  if (KIND == kUpdate) gram.init(s.pi, s.pj, a.E, J + 1, tid & 31);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + TN - 1) / TN;
   const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
@@ -315,14 +316,17 @@ __device__ __forceinline__ int upk(int i, int j, int J) {  // packed index of (i
   return i * (J + 1) - (i * (i - 1)) / 2 + (j - i);
 }
 
+// list_in == nullptr: rows 0..rows-1; else the *nlist_in rows listed
 template <class V>
-__global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf,
-                             V *__restrict__ fac, double lambda, uint32_t *__restrict__ fallback,
-                             unsigned int *__restrict__ nfallback) {
+__global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, const uint32_t *__restrict__ list_in,
+                             const unsigned int *__restrict__ nlist_in, int J, int E, int ldf, V *__restrict__ fac,
+                             double lambda, uint32_t *__restrict__ fallback, unsigned int *__restrict__ nfallback) {
   extern __shared__ double sm[];
   const int T = blockDim.x, tid = threadIdx.x;
   double *A = sm + tid;  // element e at A[e * T]
-  for (uint64_t row = (uint64_t)blockIdx.x * T + tid; row < rows; row += (uint64_t)gridDim.x * T) {
+  const uint64_t n = list_in ? (uint64_t)*nlist_in : rows;
+  for (uint64_t k0 = (uint64_t)blockIdx.x * T + tid; k0 < n; k0 += (uint64_t)gridDim.x * T) {
+    const uint64_t row = list_in ? list_in[k0] : k0;
     const double *g = gram + row * (uint64_t)E;
     for (int e = 0; e < E; ++e) A[e * T] = g[e];
     for (int i = 0; i < J; ++i) A[upk(i, i, J) * T] += lambda;
@@ -354,6 +358,93 @@ __global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, int
     } else {
       fallback[atomicAdd(nfallback, 1u)] = (uint32_t)row;
     }
+  }
+}
+
+// The precision form's row solve: FP32 Cholesky per thread (GB300 runs FP32 at
+// ~64x its FP64 rate), a condition estimate kappa ~ (max u_kk / min u_kk)^2 from
+// the factor, and one step of iterative refinement whose residual
+// r = C - (lambda I + G) a is formed from the FP64 Gram with each entry split
+// into two floats, error-free products (fmaf) and Neumaier sums.  Rows with
+// kappa above cond_max, or a non-positive pivot, go to the FP64 solver.
+__device__ __forceinline__ void neu_add(float &s, float &c, float x) {
+  const float t = s + x;
+  c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
+  s = t;
+}
+
+template <class V>
+__global__ void k_solve_rows32(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf,
+                               V *__restrict__ fac, double lambda, float cond_max, uint32_t *__restrict__ to_fp64,
+                               unsigned int *__restrict__ n_to_fp64) {
+  extern __shared__ float sf[];
+  const int T = blockDim.x, tid = threadIdx.x;
+  float *U = sf + tid;                    // packed factor, element e at U[e * T]
+  float *r = sf + (size_t)E * T + tid;    // residual / correction, element i at r[i * T]
+  const float lam = (float)lambda;
+  for (uint64_t row = (uint64_t)blockIdx.x * T + tid; row < rows; row += (uint64_t)gridDim.x * T) {
+    const double *g = gram + row * (uint64_t)E;
+    for (int e = 0; e < E; ++e) U[e * T] = (float)g[e];
+    for (int i = 0; i < J; ++i) U[upk(i, i, J) * T] = (float)(g[upk(i, i, J)] + lambda);
+    bool ok = true;
+    float umax = 0.f, umin = 3.4e38f;
+    for (int k = 0; k < J; ++k) {
+      const float d = U[upk(k, k, J) * T];
+      if (!(d > 0.f) || !isfinite(d)) {
+        ok = false;
+        break;
+      }
+      const float u = sqrtf(d), ru = 1.f / u;
+      umax = fmaxf(umax, u);
+      umin = fminf(umin, u);
+      U[upk(k, k, J) * T] = u;
+      for (int j = k + 1; j <= J; ++j) U[upk(k, j, J) * T] *= ru;
+      for (int i = k + 1; i < J; ++i) {
+        const float uki = U[upk(k, i, J) * T];
+        for (int j = i; j <= J; ++j) U[upk(i, j, J) * T] -= uki * U[upk(k, j, J) * T];
+      }
+    }
+    if (!ok || (umax / umin) * (umax / umin) > cond_max) {
+      to_fp64[atomicAdd(n_to_fp64, 1u)] = (uint32_t)row;
+      continue;
+    }
+    for (int k = J - 1; k >= 0; --k) {  // U a = y, a kept in column J
+      float v = U[upk(k, J, J) * T];
+      for (int j = k + 1; j < J; ++j) v -= U[upk(k, j, J) * T] * U[upk(j, J, J) * T];
+      U[upk(k, J, J) * T] = v / U[upk(k, k, J) * T];
+    }
+    // r = C - lambda a - G a, compensated
+    for (int i = 0; i < J; ++i) {
+      float s = 0.f, c = 0.f;
+      const double ci = g[upk(i, J, J)];
+      const float ch = (float)ci;
+      neu_add(s, c, ch);
+      neu_add(s, c, (float)(ci - (double)ch));
+      const float ai = U[upk(i, J, J) * T];
+      neu_add(s, c, -lam * ai);
+      for (int j = 0; j < J; ++j) {
+        const double gij = g[i <= j ? upk(i, j, J) : upk(j, i, J)];
+        const float gh = (float)gij, gl = (float)(gij - (double)gh);
+        const float aj = U[upk(j, J, J) * T];
+        const float ph = gh * aj;
+        const float pl = fmaf(gh, aj, -ph);
+        neu_add(s, c, -ph);
+        neu_add(s, c, -(pl + gl * aj));
+      }
+      r[i * T] = s + c;
+    }
+    for (int k = 0; k < J; ++k) {  // U^T z = r
+      float v = r[k * T];
+      for (int p = 0; p < k; ++p) v -= U[upk(p, k, J) * T] * r[p * T];
+      r[k * T] = v / U[upk(k, k, J) * T];
+    }
+    for (int k = J - 1; k >= 0; --k) {  // U d = z
+      float v = r[k * T];
+      for (int j = k + 1; j < J; ++j) v -= U[upk(k, j, J) * T] * r[j * T];
+      r[k * T] = v / U[upk(k, k, J) * T];
+    }
+    V *frow = fac + row * (uint64_t)ldf;
+    for (int j = 0; j < ldf; ++j) frow[j] = j < J ? (V)(U[upk(j, J, J) * T] + r[j * T]) : V(0);
   }
 }
 
@@ -534,6 +625,9 @@ template <class V, int KIND> bool find_spec(Launch &L, const DevTensor &t) {
 
 constexpr size_t kSmemLimit = 227 * 1024;
 constexpr int kThreadSolveMaxJ = 24;  // larger ranks solve one row per warp
+// precision form: rows whose Cholesky factor shows (max u_kk / min u_kk)^2 above
+// this are solved in FP64 (one FP32 refinement step leaves ~(kappa * 2^-24)^2)
+constexpr float kCondMaxFp32 = 1e5f;
 
 template <class V, int KIND> int choose(Launch &L, const DevTensor &t, bool &gp_in_smem) {
   gp_in_smem = true;
@@ -653,6 +747,19 @@ template <class V, int KIND> static int launch_mode(DevTensor &t, int mode, void
   return 0;
 }
 
+// the buffer for the last mode's delta ([nnz][J] value_t); without room the fit
+// recomputes delta instead (never an error)
+int ensure_dstore(DevTensor &t) {
+  if (t.dstore || t.dstore_failed || !t.nnz) return 0;
+  if (dalloc(t, &t.dstore, t.nnz * (size_t)t.J * t.vsize)) {
+    t.dstore = nullptr;
+    t.dstore_failed = true;
+    cudaGetLastError();
+    set_error("");
+  }
+  return 0;
+}
+
 template <class V> static int update_impl(DevTensor &t, int mode) {
   const int E = pairs_for(t.J);
   const int J = t.J;
@@ -660,13 +767,7 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   // the last mode's pass also stores delta, from which the sweep's fit follows exactly
   void *dstore = nullptr;
   if (last && t.nnz) {
-    if (!t.dstore && !t.dstore_failed) {
-      if (dalloc(t, &t.dstore, t.nnz * (size_t)J * sizeof(V))) {
-        t.dstore = nullptr;
-        t.dstore_failed = true;  // no room: the fit recomputes delta instead
-        cudaGetLastError();
-      }
-    }
+    if (int rc = ensure_dstore(t)) return rc;
     dstore = t.dstore;
   }
   t.fit_from_store = false;
@@ -694,8 +795,23 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
     if (int rc = prepare_fn((const void *)k_solve_rows<V>, smem)) return rc;
     uint64_t grid = (t.rows[mode] + T - 1) / T;
     if (grid < 1) grid = 1;
-    k_solve_rows<V><<<(unsigned)grid, T, smem, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf, (V *)t.fac[mode],
-                                                           kLambda, t.fallback, t.nfallback);
+    if (t.precision != GTK_PREC_PLAIN) {
+      // FP32 Cholesky + refinement; rows above the condition threshold in FP64
+      const size_t smem32 = (size_t)T * (E + J) * 4;
+      if (int rc = prepare_fn((const void *)k_solve_rows32<V>, smem32)) return rc;
+      GTK_CUDA(cudaMemsetAsync(t.nfallback + 1, 0, 4, t.stream));
+      k_solve_rows32<V><<<(unsigned)grid, T, smem32, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf,
+                                                                 (V *)t.fac[mode], kLambda, kCondMaxFp32,
+                                                                 t.fallback64, t.nfallback + 1);
+      GTK_CUDA(cudaGetLastError());
+      k_solve_rows<V><<<(unsigned)t.num_sms, T, smem, t.stream>>>(t.gram, 0, t.fallback64, t.nfallback + 1, J, E,
+                                                                  t.ldf, (V *)t.fac[mode], kLambda, t.fallback,
+                                                                  t.nfallback);
+      t.launches += 1;
+    } else {
+      k_solve_rows<V><<<(unsigned)grid, T, smem, t.stream>>>(t.gram, t.rows[mode], nullptr, nullptr, J, E, t.ldf,
+                                                             (V *)t.fac[mode], kLambda, t.fallback, t.nfallback);
+    }
     GTK_CUDA(cudaGetLastError());
     k_solve_lu_rows<V><<<(unsigned)t.num_sms, lu_wpb * 32, lu_smem, t.stream>>>(
         t.gram, t.fallback, t.nfallback, 0, J, E, t.ldf, (V *)t.fac[mode], t.status, kLambda);
@@ -718,9 +834,8 @@ int run_update_mode(DevTensor &t, int mode) {
   return t.dtype == GTK_F32 ? update_impl<float>(t, mode) : update_impl<double>(t, mode);
 }
 
-template <class V> static int fit_impl(DevTensor &t, double *fit) {
-  cudaEvent_t ev = nullptr;
-  if (int rc = prof_begin(t, &ev)) return rc;
+// the fit kernels: the error of every nonzero summed into t.partial[kFitGridMax]
+template <class V> static int fit_enqueue(DevTensor &t) {
   int grid = 1;
   if (t.fit_from_store && t.nnz) {
     grid = (int)std::min<uint64_t>(kFitGridMax, (t.nnz + 255) / 256);
@@ -741,7 +856,10 @@ template <class V> static int fit_impl(DevTensor &t, double *fit) {
   k_sum_fit<<<1, 32, 0, t.stream>>>(t.partial, grid, t.partial + kFitGridMax);
   GTK_CUDA(cudaGetLastError());
   t.launches += 1;
-  if (int rc = prof_end(t, 2, ev)) return rc;
+  return 0;
+}
+
+static int fit_read(DevTensor &t, double *fit) {
   double err = 0;
   GTK_CUDA(cudaMemcpyAsync(&err, t.partial + kFitGridMax, 8, cudaMemcpyDeviceToHost, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
@@ -749,7 +867,65 @@ template <class V> static int fit_impl(DevTensor &t, double *fit) {
   return 0;
 }
 
-int run_fit(DevTensor &t, double *fit) { return t.dtype == GTK_F32 ? fit_impl<float>(t, fit) : fit_impl<double>(t, fit); }
+int run_fit(DevTensor &t, double *fit) {
+  cudaEvent_t ev = nullptr;
+  if (int rc = prof_begin(t, &ev)) return rc;
+  if (int rc = t.dtype == GTK_F32 ? fit_enqueue<float>(t) : fit_enqueue<double>(t)) return rc;
+  if (int rc = prof_end(t, 2, ev)) return rc;
+  return fit_read(t, fit);
+}
+
+void drop_graph(DevTensor &t) {
+  if (t.gexec) cudaGraphExecDestroy(t.gexec);
+  if (t.graph) cudaGraphDestroy(t.graph);
+  t.gexec = nullptr;
+  t.graph = nullptr;
+}
+
+// One sweep (every mode's update, then the fit).  With t.use_graph the device
+// work of a sweep -- memsets, the fused and solve kernels of every mode, the fit
+// kernels -- is captured once into a CUDA graph and replayed; only the 8-byte
+// read of the error sum stays outside.
+int run_sweep(DevTensor &t, double *fit) {
+  if (!t.use_graph) {
+    for (int n = 0; n < t.N; ++n)
+      if (int rc = run_update_mode(t, n)) return rc;
+    return run_fit(t, fit);
+  }
+  if (!t.gexec) {
+    if (int rc = ensure_dstore(t)) return rc;
+    const bool prof = t.prof;
+    t.prof = false;
+    const uint64_t l0 = t.launches;
+    GTK_CUDA(cudaStreamBeginCapture(t.stream, cudaStreamCaptureModeThreadLocal));
+    int rc = 0;
+    for (int n = 0; n < t.N && !rc; ++n) rc = run_update_mode(t, n);
+    if (!rc) rc = t.dtype == GTK_F32 ? fit_enqueue<float>(t) : fit_enqueue<double>(t);
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(t.stream, &g);
+    t.prof = prof;
+    if (rc || ec != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      t.launches = l0;
+      return rc ? rc : cuda_fail(ec, "cudaStreamEndCapture");
+    }
+    t.graph = g;
+    if (cudaGraphInstantiate(&t.gexec, t.graph, 0) != cudaSuccess) {
+      drop_graph(t);
+      return cuda_fail(cudaGetLastError(), "cudaGraphInstantiate");
+    }
+    t.graph_kernels = t.launches - l0;
+    t.launches = l0;
+  }
+  cudaEvent_t ev = nullptr;
+  if (int rc = prof_begin(t, &ev)) return rc;
+  GTK_CUDA(cudaGraphLaunch(t.gexec, t.stream));
+  if (int rc = prof_end(t, 3, ev)) return rc;
+  t.launches += t.graph_kernels;
+  t.fit_from_store = t.dstore != nullptr;
+  return fit_read(t, fit);
+}
 
 int run_delta(DevTensor &t, int mode, void *d_out) {
   if (!t.nnz) return 0;

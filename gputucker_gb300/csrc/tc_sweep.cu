@@ -149,7 +149,7 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int SBO = (KP / EPC) * 128;  // bytes between 8-row groups
   static constexpr int A_BYTES = kTcThreads * KP * ES;
   static constexpr int B_BYTES = NP * KP * ES;
-  static constexpr int LDD = ((J + 1) & 1) ? J + 1 : J + 2;
+  static constexpr int LDD = ((J + 2) & 1) ? J + 2 : J + 3;  // column J + 1 stays zero
   static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
   static constexpr int OFF_B = A_BYTES;
   static constexpr int OFF_DX = (OFF_B + B_BYTES + 15) / 16 * 16;
@@ -217,8 +217,10 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   double err = 0;
   uint32_t phase = 0;
   bool timed_out = false;
-  GramAcc<float, gram_slots(J)> gram;
-  if (KIND == 0) gram.init(ts.pi, ts.pj, S::E, tid & 31);
+  GramAcc<float, gram_slots(J), false> gram;
+  for (int k = tid; k < kTcThreads; k += kTcThreads) ts.dx[k * S::LDD + J + 1] = 0.f;
+  __syncthreads();
+  if (KIND == 0) gram.init(ts.pi, ts.pj, S::E, J + 1, tid & 31);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
   const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
@@ -308,19 +310,23 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
     float delta[J];
 #pragma unroll
     for (int j = 0; j < J; ++j) delta[j] = 0.f;
+    {
+      float v[S::NP / 16][16];  // the whole lane of the accumulator: all loads, then one wait
 #pragma unroll
-    for (int c = 0; c < S::NP / 16; ++c) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v);
+      for (int c = 0; c < S::NP / 16; ++c)
+        tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v[c]);
       tmem_wait_ld();
 #pragma unroll
-      for (int i = 0; i < 16; ++i) {
-        const int col = c * 16 + i;
-        if (col < S::ND) {
-          if (D == 2)
-            delta[col] = v[i];
-          else
-            delta[col / J] += cur.e1[col % J] * v[i];
+      for (int c = 0; c < S::NP / 16; ++c) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+          const int col = c * 16 + i;
+          if (col < S::ND) {
+            if (D == 2)
+              delta[col] = v[c][i];
+            else
+              delta[col / J] += cur.e1[col % J] * v[c][i];
+          }
         }
       }
     }

@@ -247,6 +247,15 @@ class BlockedTensor:
         call("gtk_reconstruction", self.handle, C.byref(f))
         return f.value
 
+    def sweep(self) -> float:
+        """One ALS sweep (all modes) and its fit; replays a CUDA graph when set_graph(True)."""
+        f = C.c_double()
+        call("gtk_sweep", self.handle, C.byref(f))
+        return f.value
+
+    def set_graph(self, on: bool = True) -> None:
+        call("gtk_set_graph", self.handle, 1 if on else 0)
+
     def tucker_decomposition(self, max_iters: int = 3, tol: float = 1e-4) -> list:
         fits = (C.c_double * max_iters)()
         it = C.c_int()

@@ -150,6 +150,14 @@ int gtk_reconstruction(gtk_tensor *t, double *fit);
  * |fit - previous fit| <= tol (the reference: 3 sweeps, tol = lambda = 1e-4).
  * fits[i] receives the fit of sweep i (array of max_iters), *iters the sweeps run. */
 int gtk_tucker_decomposition(gtk_tensor *t, int max_iters, double tol, double *fits, int *iters);
+/* one sweep: gtk_update_factor_matrices then gtk_reconstruction */
+int gtk_sweep(gtk_tensor *t, double *fit);
+/* No reference counterpart.  on != 0: gtk_sweep (and gtk_tucker_decomposition)
+ * capture the device work of a sweep -- every mode's kernels and the fit
+ * kernels -- into a CUDA graph on first use and replay it afterwards; changing
+ * the precision drops the graph.  Factor and core contents may change freely
+ * between replays (the graph holds the handle's buffers, not their values). */
+int gtk_set_graph(gtk_tensor *t, int on);
 /* the delta of every nonzero for `mode` with the current factors, [nnz][J] in
  * block-major order (the reference's per-block delta buffers concatenated,
  * delta.cuh:206).  A parity hook: the sweep itself never writes delta to HBM. */
@@ -178,7 +186,9 @@ int gtk_write_text(const gtk_coo *coo, const char *path);
 
 /* ---- timing ----------------------------------------------------------- */
 /* Per-kernel device time accumulated with CUDA events on the handle's stream
- * while enabled.  kind: 0 delta+gram, 1 solve, 2 fit, 3 all sweep kernels. */
+ * while enabled.  kind: 0 delta+gram, 1 solve, 2 fit, 3 whole sweeps replayed
+ * from a graph (gtk_set_graph); kind 4 reads the number of kernels the sweep
+ * entry points launched (ms = 0). */
 int gtk_profile_enable(gtk_tensor *t, int on);
 int gtk_profile_read(gtk_tensor *t, int kind, double *ms, uint64_t *launches);
 int gtk_profile_reset(gtk_tensor *t);
