@@ -13,6 +13,13 @@ namespace gtk {
 
 constexpr int kMaxOrder = GTK_MAX_ORDER;
 constexpr int kMaxRank = GTK_MAX_RANK;
+// update-kernel variants (the autotuner's search space)
+constexpr int kVarAuto = -1;    // specialised NPT = 2 (plain) / tensor cores (precision forms)
+constexpr int kVarSpec2 = 0;    // specialised SIMT kernel, 2 nonzeros per thread
+constexpr int kVarSpec1 = 1;    // specialised SIMT kernel, 1 nonzero per thread
+constexpr int kVarGeneric = 2;  // runtime-(N, J) SIMT kernel
+constexpr int kVarTc = 3;       // tcgen05 kernel (precision forms)
+constexpr int kFitSumSlot = 1024;  // partial[] index of a fit's error sum
 // constants.hpp:18 declares kLambda as a double initialised from the float
 // literal 0.0001f, so its value is float(1e-4) widened to double.
 constexpr double kLambda = (double)0.0001f;
@@ -130,6 +137,7 @@ struct DevTensor {
   uint32_t *fallback64 = nullptr; // precision form: rows re-solved in FP64
   unsigned int *nfallback = nullptr;
   uint64_t launches = 0;        // kernels launched by the sweep entry points
+  int variant = -1;             // update kernel: kVarAuto or one the autotuner picked
   bool use_graph = false;       // gtk_sweep replays a captured CUDA graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -157,6 +165,7 @@ int run_update_mode(DevTensor &t, int mode);
 int run_fit(DevTensor &t, double *fit);
 int run_delta(DevTensor &t, int mode, void *d_delta_blockmajor);
 int run_sweep(DevTensor &t, double *fit);
+int run_fit_enqueue(DevTensor &t);  // the fit kernels only; the sum lands in partial[kFitSumSlot]
 int ensure_dstore(DevTensor &t);
 void drop_graph(DevTensor &t);
 // tc_sweep.cu: the tensor-core (BF16 / TF32) form; kind 0 update, 1 fit, 2 delta

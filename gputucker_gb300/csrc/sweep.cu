@@ -595,8 +595,7 @@ struct Launch {
 };
 
 
-template <class V, int N, int J, int KIND> void spec_entry(Launch &L, const DevTensor &t) {
-  constexpr int NPT = 2;
+template <class V, int N, int J, int KIND, int NPT> void spec_entry(Launch &L, const DevTensor &t) {
   constexpr int W = Vec<V>::W;
   constexpr int LDG = (J + W - 1) / W * W;
   constexpr int D = N - 1;
@@ -609,11 +608,11 @@ template <class V, int N, int J, int KIND> void spec_entry(Launch &L, const DevT
   (void)t;
 }
 
-// The specialised (N, J) table.  Anything else runs the generic kernel.
-template <class V, int KIND> bool find_spec(Launch &L, const DevTensor &t) {
+// The specialised (N, J) table (NPT nonzeros per thread).  Anything else runs the generic kernel.
+template <class V, int KIND, int NPT> bool find_spec(Launch &L, const DevTensor &t) {
 #define GTK_SPEC(NN, JJ)                                          \
   if (t.N == NN && t.J == JJ) {                                   \
-    spec_entry<V, NN, JJ, KIND>(L, t);                            \
+    spec_entry<V, NN, JJ, KIND, NPT>(L, t);                       \
     return true;                                                  \
   }
   GTK_SPEC(3, 4) GTK_SPEC(3, 8) GTK_SPEC(3, 10) GTK_SPEC(3, 12) GTK_SPEC(3, 16)
@@ -629,9 +628,15 @@ constexpr int kThreadSolveMaxJ = 24;  // larger ranks solve one row per warp
 // this are solved in FP64 (one FP32 refinement step leaves ~(kappa * 2^-24)^2)
 constexpr float kCondMaxFp32 = 1e5f;
 
+// kernel of a KIND: the update honours the handle's variant (set by the autotuner)
 template <class V, int KIND> int choose(Launch &L, const DevTensor &t, bool &gp_in_smem) {
   gp_in_smem = true;
-  if (find_spec<V, KIND>(L, t) && L.smem <= kSmemLimit) return 0;
+  const int var = KIND == kUpdate ? t.variant : kVarAuto;
+  if (var == kVarSpec1) {
+    if (find_spec<V, KIND, 1>(L, t) && L.smem <= kSmemLimit) return 0;
+  } else if (var != kVarGeneric) {
+    if (find_spec<V, KIND, 2>(L, t) && L.smem <= kSmemLimit) return 0;
+  }
   const size_t gp = (size_t)t.core_n / (size_t)t.J * t.ldf;
   L.spec = false;
   L.tn = kThreads;
@@ -775,7 +780,8 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   if (int rc = prof_begin(t, &ev)) return rc;
   GTK_CUDA(cudaMemsetAsync(t.gram, 0, t.rows[mode] * (uint64_t)E * 8, t.stream));
   if (t.nnz) {
-    if (t.precision != GTK_PREC_PLAIN) {
+    const bool tc = t.variant == kVarTc || (t.variant == kVarAuto && t.precision != GTK_PREC_PLAIN);
+    if (tc) {
       if (int rc = run_mode_tc(t, mode, 0, dstore, nullptr)) return rc;
     } else if (int rc = launch_mode<V, kUpdate>(t, mode, dstore, nullptr)) {
       return rc;
@@ -866,6 +872,8 @@ static int fit_read(DevTensor &t, double *fit) {
   *fit = (t.norm == 0) ? 1.0 : 1.0 - std::sqrt(err) / t.norm;
   return 0;
 }
+
+int run_fit_enqueue(DevTensor &t) { return t.dtype == GTK_F32 ? fit_enqueue<float>(t) : fit_enqueue<double>(t); }
 
 int run_fit(DevTensor &t, double *fit) {
   cudaEvent_t ev = nullptr;

@@ -4,8 +4,10 @@
   configuration the reference runs end to end; held against the FP64 oracle
   (the reference's CPU path) for 3 sweeps at full size.
 * 3-order Zipf(1.05) lognormal precision configuration (rank 16): BF16 and TF32
-  tensor-core forms against plain FP32 on a 20M-nonzero instance (the 500M
-  instance is measured, not tested: the oracle cannot follow it).
+  tensor-core forms against plain FP32 on a 20M-nonzero instance whose dims are
+  scaled with the nonzeros (40,000^3: ~500 nonzeros per row, as 500M over
+  1,000,000^3 has; at 20M over 10^6 rows most rows are under-determined and every
+  form, plain FP32 included, oscillates).
 * size-independent properties of the 4-order 100M configuration's partition on
   a 10M instance: every block's where_nnz is a permutation sorted by its row
   pointer, count_nnz sums to the block size.
@@ -38,7 +40,7 @@ def test_config_uniform3d_1m_fp64_full_size():
 
 
 def test_config_precision3d_forms_agree():
-    coo = gtk.generate(3, [1_000_000] * 3, 20_000_000, "zipf", 1.05, "lognormal", "f32", seed=0)
+    coo = gtk.generate(3, [40_000] * 3, 20_000_000, "zipf", 1.05, "lognormal", "f32", seed=0)
     fits = {}
     with gtk.create_tensor_blocks(coo, [1, 1, 1], 16) as t:
         for prec in ("plain", "bf16", "tf32"):
