@@ -100,6 +100,8 @@ SIGNATURES = {
     "gtk_generate_planted": (C.c_int, [C.c_int, U32P, C.c_uint64, C.c_int, C.c_double, C.c_int, C.c_uint64,
                                        C.POINTER(P)]),
     "gtk_write_text": (C.c_int, [P, C.c_char_p]),
+    "gtk_reconstruction_error_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.POINTER(P), P, C.POINTER(P), P, P,
+                                                   P]),
     "gtk_profile_enable": (C.c_int, [P, C.c_int]),
     "gtk_profile_read": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), U64P]),
     "gtk_profile_reset": (C.c_int, [P]),

@@ -163,6 +163,27 @@ int gtk_set_graph(gtk_tensor *t, int on);
  * delta.cuh:206).  A parity hook: the sweep itself never writes delta to HBM. */
 int gtk_compute_delta(gtk_tensor *t, int mode, void *delta);
 
+/* ---- no device allocation ----------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory where they run -- work recorded into a CUDA graph by stream capture,
+ * allocator-free latency-critical loops, device memory owned by another
+ * runtime's pool: the sum of squared reconstruction errors sum_t (x_t - x_hat_t)^2
+ * of caller-owned device data, written to d_err (one double in device memory)
+ * by kernels enqueued on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream).  FP32 data: d_idx[n] -> nnz 0-based coordinates of mode n, d_vals ->
+ * nnz values, d_factors[n] -> (largest index of mode n + 1) x rank row-major,
+ * d_core -> rank^order values, last mode fastest (the arrays are device
+ * pointers; the two pointer tables are host arrays).  fit = 1 - sqrt(err)/||X||.
+ * Allocates nothing: the kernels' scratch is a fixed device array of
+ * 8 KB + 4 MB inside the library, held on every GPU that loads it, so
+ * rank^(order-1) * round_up(rank, 4) must not exceed 2^20 (else
+ * GTK_ERR_UNSUPPORTED).  The first call on a device looks the array up; make it
+ * before any stream capture starts.  Calls whose kernels overlap on the GPU
+ * share the array and race: serialise them. */
+int gtk_reconstruction_error_noalloc(int order, int rank, uint64_t nnz, const uint32_t *const *d_idx,
+                                     const float *d_vals, const float *const *d_factors, const float *d_core,
+                                     double *d_err, void *stream);
+
 /* ---- data on either side of the path ----------------------------------
  * No reference counterpart: the reference only reads files it did not make.
  * gtk_generate draws `nnz` distinct coordinates (each mode uniform, or
