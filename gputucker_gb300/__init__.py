@@ -7,6 +7,7 @@ is a thin host binding over it.
 
 from ._native import GTKError, LIB_PATH  # noqa: F401
 from .tucker import (  # noqa: F401
+    Batch,
     BlockedTensor,
     Coo,
     coo_from_arrays,
@@ -19,6 +20,6 @@ from .tucker import (  # noqa: F401
 )
 
 __all__ = [
-    "GTKError", "LIB_PATH", "BlockedTensor", "Coo", "coo_from_arrays", "create_tensor_blocks", "generate",
+    "GTKError", "LIB_PATH", "Batch", "BlockedTensor", "Coo", "coo_from_arrays", "create_tensor_blocks", "generate",
     "generate_planted", "parse_buffer", "parse_from_file", "tucker_decomposition",
 ]

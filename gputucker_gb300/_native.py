@@ -102,6 +102,13 @@ SIGNATURES = {
     "gtk_write_text": (C.c_int, [P, C.c_char_p]),
     "gtk_reconstruction_error_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.POINTER(P), P, C.POINTER(P), P, P,
                                                    P]),
+    "gtk_set_kernel_variant": (C.c_int, [P, C.c_int]),
+    "gtk_get_kernel_variant": (C.c_int, [P, C.POINTER(C.c_int)]),
+    "gtk_autotune": (C.c_int, [P, C.POINTER(C.c_int)]),
+    "gtk_batch_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),
+    "gtk_batch_sweep": (C.c_int, [P, C.POINTER(C.c_double)]),
+    "gtk_batch_kernels": (C.c_int, [P, U64P]),
+    "gtk_batch_destroy": (None, [P]),
     "gtk_profile_enable": (C.c_int, [P, C.c_int]),
     "gtk_profile_read": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), U64P]),
     "gtk_profile_reset": (C.c_int, [P]),

@@ -474,6 +474,7 @@ int gtk_set_precision(gtk_tensor *t, int precision) {
     return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this order/rank/value type (FP32, N = 3 or 4, "
                                      "J in {4, 8, 10, 12, 16} for N = 3 and {4, 8, 10, 12} for N = 4)");
   t->precision = precision;
+  if (precision == GTK_PREC_PLAIN && t->variant == kVarTc) t->variant = kVarAuto;
   return 0;
 }
 

@@ -19,6 +19,9 @@ constexpr int kVarSpec2 = 0;    // specialised SIMT kernel, 2 nonzeros per threa
 constexpr int kVarSpec1 = 1;    // specialised SIMT kernel, 1 nonzero per thread
 constexpr int kVarGeneric = 2;  // runtime-(N, J) SIMT kernel
 constexpr int kVarTc = 3;       // tcgen05 kernel (precision forms)
+static_assert(kVarAuto == GTK_VARIANT_AUTO && kVarSpec2 == GTK_VARIANT_SIMT2 && kVarSpec1 == GTK_VARIANT_SIMT1 &&
+                  kVarGeneric == GTK_VARIANT_GENERIC && kVarTc == GTK_VARIANT_TENSOR_CORE,
+              "variant codes of the C ABI");
 constexpr int kFitSumSlot = 1024;  // partial[] index of a fit's error sum
 // constants.hpp:18 declares kLambda as a double initialised from the float
 // literal 0.0001f, so its value is float(1e-4) widened to double.
@@ -166,6 +169,7 @@ int run_fit(DevTensor &t, double *fit);
 int run_delta(DevTensor &t, int mode, void *d_delta_blockmajor);
 int run_sweep(DevTensor &t, double *fit);
 int run_fit_enqueue(DevTensor &t);  // the fit kernels only; the sum lands in partial[kFitSumSlot]
+int run_row_stats(DevTensor &t, int mode, uint32_t *max_count);
 int ensure_dstore(DevTensor &t);
 void drop_graph(DevTensor &t);
 // tc_sweep.cu: the tensor-core (BF16 / TF32) form; kind 0 update, 1 fit, 2 delta

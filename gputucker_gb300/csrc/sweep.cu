@@ -33,6 +33,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -94,9 +95,30 @@ template <class V, int J, int LDG, int NPT> struct Nest<V, J, LDG, NPT, 2> {
 };
 
 
+// ---------------------------------------------------------------- core streaming
+// 16-byte asynchronous global->shared copies (cp.async, completion by groups)
+__device__ __forceinline__ void cp_async16(void *sdst, const void *gsrc) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Cores too large for shared memory (J^(N-1) * LDG values above ~200 KB) are
+// streamed: chunk c is J^2 rows of LDG values -- for N = 4 the slice of one
+// mode-n index jn, for N = 5 the slice of one (jn, first other index) pair -- the
+// input of one Nest<3>.  Two chunk buffers; chunk c+1 is in flight while chunk c
+// is contracted.
+template <int N, int J, int LDG> struct CoreStream {
+  static constexpr int D = N - 1;
+  static constexpr int NC = D == 3 ? J : J * J;       // chunks per pass over the core
+  static constexpr size_t CH = (size_t)J * J * LDG;  // values per chunk
+};
+
 // ---------------------------------------------------------------- specialised kernel
 // Compile-time order N and rank J; NPT nonzeros per thread share every core read.
-template <class V, int N, int J, int NPT, int KIND>
+// STREAM: the core is streamed through shared memory in chunks (CoreStream).
+template <class V, int N, int J, int NPT, int KIND, bool STREAM = false>
 __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
   using VT = typename Vec<V>::T;
   constexpr int W = Vec<V>::W;
@@ -104,11 +126,14 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
   constexpr int D = N - 1;                 // other modes
   constexpr int LEV = D > 2 ? D - 2 : 0;   // outer levels with factor rows in shared memory
   constexpr int TN = kThreads * NPT;
-  constexpr size_t GP = (size_t)Pow<J, N - 1>::v * LDG;
+  using CS = CoreStream<N, J, LDG>;
+  static_assert(!STREAM || D == 3 || D == 4, "streamed core: N = 4 or 5");
+  static_assert(!STREAM || (CS::CH * sizeof(V)) % 16 == 0, "chunks move in 16-byte pieces");
+  constexpr size_t GP = STREAM ? 2 * CS::CH : (size_t)Pow<J, N - 1>::v * LDG;
   extern __shared__ __align__(16) unsigned char smem[];
   const TileSmem<V> s = carve<V>(smem, GP, LEV, NPT, J, a.ldd, a.E, TN);
   const int tid = threadIdx.x;
-  {
+  if (!STREAM) {
     const VT *src = reinterpret_cast<const VT *>(a.corep);
     VT *dst = reinterpret_cast<VT *>(s.gp);
     for (size_t k = tid; k < GP / W; k += kThreads) dst[k] = src[k];
@@ -162,10 +187,8 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
     V xhat[NPT];
 #pragma unroll
     for (int q = 0; q < NPT; ++q) xhat[q] = V(0);
-#pragma unroll 1
-    for (int jn = 0; jn < J; ++jn) {
-      V o[NPT];
-      Nest<V, J, LDG, NPT, D>::run(s.gp + (size_t)jn * Pow<J, N - 2>::v * LDG, s.arow + tid, lvl_stride, a1, a2, o);
+    // delta_jn of the thread's nonzeros is o: store / use it
+    auto finish = [&](int jn, const V (&o)[NPT]) {
 #pragma unroll
       for (int q = 0; q < NPT; ++q) {
         const int tl = q * kThreads + tid;
@@ -176,6 +199,52 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
         } else {
           if (tl < nv) reinterpret_cast<V *>(a.out)[(size_t)a.vperm[t0 + tl] * J + jn] = o[q];
         }
+      }
+    };
+    if constexpr (!STREAM) {
+#pragma unroll 1
+      for (int jn = 0; jn < J; ++jn) {
+        V o[NPT];
+        Nest<V, J, LDG, NPT, D>::run(s.gp + (size_t)jn * Pow<J, N - 2>::v * LDG, s.arow + tid, lvl_stride, a1, a2,
+                                     o);
+        finish(jn, o);
+      }
+    } else {
+      const V *core = reinterpret_cast<const V *>(a.corep);
+      auto issue = [&](int c) {
+        const char *src = reinterpret_cast<const char *>(core + (size_t)c * CS::CH);
+        char *dst = reinterpret_cast<char *>(s.gp + (size_t)(c & 1) * CS::CH);
+        constexpr int P16 = (int)(CS::CH * sizeof(V) / 16);
+        for (int k = tid; k < P16; k += kThreads) cp_async16(dst + 16 * k, src + 16 * k);
+      };
+      issue(0);
+      cp_async_commit();
+      V o[NPT];
+#pragma unroll
+      for (int q = 0; q < NPT; ++q) o[q] = V(0);
+#pragma unroll 1
+      for (int c = 0; c < CS::NC; ++c) {
+        if (c + 1 < CS::NC) issue(c + 1);
+        cp_async_commit();  // possibly empty: the group count stays one ahead
+        cp_async_wait1();   // chunk c has landed (this thread's copies)
+        __syncthreads();    // ... and every thread's
+        const V *g = s.gp + (size_t)(c & 1) * CS::CH;
+        if constexpr (D == 3) {
+          Nest<V, J, LDG, NPT, 3>::run(g, s.arow + tid, lvl_stride, a1, a2, o);
+          finish(c, o);
+        } else {
+          const int j0 = c % J;
+          V sub[NPT];
+          Nest<V, J, LDG, NPT, 3>::run(g, s.arow + tid + lvl_stride, lvl_stride, a1, a2, sub);
+#pragma unroll
+          for (int q = 0; q < NPT; ++q) o[q] += s.arow[(q * J + j0) * kThreads + tid] * sub[q];
+          if (j0 == J - 1) {
+            finish(c / J, o);
+#pragma unroll
+            for (int q = 0; q < NPT; ++q) o[q] = V(0);
+          }
+        }
+        __syncthreads();  // chunk buffer c & 1 is refilled by the issue of chunk c + 2
       }
     }
     if (KIND == kUpdate) {
@@ -595,13 +664,14 @@ struct Launch {
 };
 
 
-template <class V, int N, int J, int KIND, int NPT> void spec_entry(Launch &L, const DevTensor &t) {
+template <class V, int N, int J, int KIND, int NPT, bool STREAM = false>
+void spec_entry(Launch &L, const DevTensor &t) {
   constexpr int W = Vec<V>::W;
   constexpr int LDG = (J + W - 1) / W * W;
   constexpr int D = N - 1;
   constexpr int LEV = D > 2 ? D - 2 : 0;
-  const size_t gp = (size_t)Pow<J, N - 1>::v * LDG;
-  L.fn = (const void *)k_mode_spec<V, N, J, NPT, KIND>;
+  const size_t gp = STREAM ? 2 * CoreStream<N, J, LDG>::CH : (size_t)Pow<J, N - 1>::v * LDG;
+  L.fn = (const void *)k_mode_spec<V, N, J, NPT, KIND, STREAM>;
   L.smem = tile_smem_bytes(sizeof(V), gp, LEV, NPT, J, ldd_for(J), pairs_for(J), kThreads * NPT);
   L.tn = kThreads * NPT;
   L.spec = true;
@@ -619,6 +689,16 @@ template <class V, int KIND, int NPT> bool find_spec(Launch &L, const DevTensor 
   GTK_SPEC(4, 4) GTK_SPEC(4, 8) GTK_SPEC(4, 10) GTK_SPEC(4, 12)
   GTK_SPEC(5, 4) GTK_SPEC(5, 8)
 #undef GTK_SPEC
+  // cores streamed through shared memory (FP32 update and fit)
+  if constexpr (std::is_same<V, float>::value && KIND != kDelta) {
+#define GTK_STREAM(NN, JJ)                                        \
+  if (t.N == NN && t.J == JJ) {                                   \
+    spec_entry<V, NN, JJ, KIND, NPT, true>(L, t);                 \
+    return true;                                                  \
+  }
+    GTK_STREAM(4, 16) GTK_STREAM(5, 12) GTK_STREAM(5, 16)
+#undef GTK_STREAM
+  }
   return false;
 }
 
@@ -873,6 +953,7 @@ static int fit_read(DevTensor &t, double *fit) {
   return 0;
 }
 
+static_assert(kFitSumSlot == kFitGridMax, "the fit's error sum follows the per-CTA partials");
 int run_fit_enqueue(DevTensor &t) { return t.dtype == GTK_F32 ? fit_enqueue<float>(t) : fit_enqueue<double>(t); }
 
 int run_fit(DevTensor &t, double *fit) {
@@ -940,6 +1021,37 @@ int run_delta(DevTensor &t, int mode, void *d_out) {
   if (t.precision != GTK_PREC_PLAIN) return run_mode_tc(t, mode, 2, d_out, nullptr);
   return t.dtype == GTK_F32 ? launch_mode<float, kDelta>(t, mode, d_out, nullptr)
                             : launch_mode<double, kDelta>(t, mode, d_out, nullptr);
+}
+
+// the longest row of `mode` (number of nonzeros), for the autotuner's shape key
+__global__ void k_row_count(const uint32_t *__restrict__ row_of, uint64_t nnz, uint32_t *__restrict__ cnt) {
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nnz; t += (uint64_t)gridDim.x * blockDim.x)
+    atomicAdd(&cnt[row_of[t]], 1u);
+}
+__global__ void k_max_u32(const uint32_t *__restrict__ a, uint64_t n, uint32_t *__restrict__ out) {
+  uint32_t m = 0;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x)
+    m = max(m, a[t]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xFFFFFFFFu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+int run_row_stats(DevTensor &t, int mode, uint32_t *max_count) {
+  *max_count = 0;
+  if (!t.nnz) return 0;
+  uint32_t *cnt = nullptr;
+  GTK_CUDA(cudaMalloc(&cnt, (t.rows[mode] + 1) * 4));
+  int rc = ck(cudaMemsetAsync(cnt, 0, (t.rows[mode] + 1) * 4, t.stream), "memset");
+  if (!rc) {
+    k_row_count<<<t.num_sms * 8, 256, 0, t.stream>>>(t.vidx[mode][mode], t.nnz, cnt);
+    k_max_u32<<<t.num_sms * 4, 256, 0, t.stream>>>(cnt, t.rows[mode], cnt + t.rows[mode]);
+    rc = ck(cudaGetLastError(), "row stats");
+  }
+  if (!rc) rc = ck(cudaMemcpyAsync(max_count, cnt + t.rows[mode], 4, cudaMemcpyDeviceToHost, t.stream), "d2h");
+  if (!rc) rc = ck(cudaStreamSynchronize(t.stream), "sync");
+  cudaFree(cnt);
+  return rc;
 }
 
 // Builds G_n (mode n first, the other modes in increasing order, the last one

@@ -24,6 +24,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <vector>
 
 #include "internal.h"
 #include "mode_common.cuh"
@@ -406,7 +407,28 @@ template <int KIND> bool tc_choose(TcLaunch &L, int prec, int N, int J) {
   return prec == GTK_PREC_BF16 ? tc_find<GTK_PREC_BF16, KIND>(L, N, J) : tc_find<GTK_PREC_TF32, KIND>(L, N, J);
 }
 
+int tc_prepare_uncached(const TcLaunch &L, int num_sms, int *grid_cap, int *smem_out);
+
+// cached per kernel: no CUDA call after the first launch of a kernel (launches
+// recorded into a CUDA graph then issue no attribute calls)
 int tc_prepare(const TcLaunch &L, int num_sms, int *grid_cap, int *smem_out) {
+  struct Entry {
+    const void *fn;
+    int sms, cap, smem;
+  };
+  static std::vector<Entry> cache;
+  for (const Entry &e : cache)
+    if (e.fn == L.fn && e.sms == num_sms) {
+      *grid_cap = e.cap;
+      *smem_out = e.smem;
+      return 0;
+    }
+  if (int rc = tc_prepare_uncached(L, num_sms, grid_cap, smem_out)) return rc;
+  cache.push_back({L.fn, num_sms, *grid_cap, *smem_out});
+  return 0;
+}
+
+int tc_prepare_uncached(const TcLaunch &L, int num_sms, int *grid_cap, int *smem_out) {
   // at most 512 / ncols CTAs may share an SM's TMEM: request enough shared
   // memory that no more than that many fit, so tcgen05.alloc never has to wait
   const int max_ctas = 512 / L.ncols;

@@ -256,6 +256,23 @@ class BlockedTensor:
     def set_graph(self, on: bool = True) -> None:
         call("gtk_set_graph", self.handle, 1 if on else 0)
 
+    VARIANTS = {"auto": -1, "simt2": 0, "simt1": 1, "generic": 2, "tensor_core": 3}
+
+    def set_kernel_variant(self, variant: str) -> None:
+        """Force the update kernel ('auto', 'simt2', 'simt1', 'generic', 'tensor_core')."""
+        call("gtk_set_kernel_variant", self.handle, self.VARIANTS[variant])
+
+    def kernel_variant(self) -> str:
+        v = C.c_int()
+        call("gtk_get_kernel_variant", self.handle, C.byref(v))
+        return {c: n for n, c in self.VARIANTS.items()}[v.value]
+
+    def autotune(self) -> str:
+        """Time the applicable update kernels on mode 0 and keep the fastest (factors unchanged)."""
+        v = C.c_int()
+        call("gtk_autotune", self.handle, C.byref(v))
+        return {c: n for n, c in self.VARIANTS.items()}[v.value]
+
     def tucker_decomposition(self, max_iters: int = 3, tol: float = 1e-4) -> list:
         fits = (C.c_double * max_iters)()
         it = C.c_int()
@@ -293,6 +310,46 @@ class BlockedTensor:
     def close(self) -> None:
         if self._h is not None:
             nat.load().gtk_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Batch:
+    """Several BlockedTensors on one device swept together (gtk_batch_*): the first
+    sweep runs eagerly, later ones replay one CUDA graph in which every tensor's
+    sweep is an independent branch.  Close the batch before its tensors."""
+
+    def __init__(self, tensors):
+        self.tensors = list(tensors)
+        tab = (C.c_void_p * len(self.tensors))(*[t.handle for t in self.tensors])
+        h = C.c_void_p()
+        call("gtk_batch_create", tab, len(self.tensors), C.byref(h))
+        self._h = h
+
+    def sweep(self) -> np.ndarray:
+        fits = (C.c_double * len(self.tensors))()
+        call("gtk_batch_sweep", self._h, fits)
+        return np.array(fits[:], dtype=np.float64)
+
+    def kernels(self) -> int:
+        n = C.c_uint64()
+        call("gtk_batch_kernels", self._h, C.byref(n))
+        return n.value
+
+    def close(self) -> None:
+        if self._h is not None:
+            nat.load().gtk_batch_destroy(self._h)
             self._h = None
 
     def __enter__(self):

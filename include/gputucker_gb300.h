@@ -163,6 +163,39 @@ int gtk_set_graph(gtk_tensor *t, int on);
  * delta.cuh:206).  A parity hook: the sweep itself never writes delta to HBM. */
 int gtk_compute_delta(gtk_tensor *t, int mode, void *delta);
 
+/* ---- kernel variants, autotuner, batches -------------------------------
+ * No reference counterpart.  The update kernel of a handle is one of:
+ * GTK_VARIANT_SIMT2 / SIMT1 (specialised SIMT kernels, 2 or 1 nonzeros per
+ * thread; shapes without a specialisation run GENERIC), GTK_VARIANT_GENERIC
+ * (runtime order and rank), GTK_VARIANT_TENSOR_CORE (tcgen05; needs a precision
+ * form).  GTK_VARIANT_AUTO: tensor cores for the precision forms, SIMT2
+ * otherwise.  gtk_set_kernel_variant forces one; gtk_autotune times the variants
+ * that apply on the handle's mode-0 update (factor 0 restored afterwards), keeps
+ * the fastest and caches it per (order, rank, value type, precision, log2 mean
+ * row length, log2 longest/mean row length) for the process, so later handles
+ * of the same class skip the timing. */
+#define GTK_VARIANT_AUTO (-1)
+#define GTK_VARIANT_SIMT2 0
+#define GTK_VARIANT_SIMT1 1
+#define GTK_VARIANT_GENERIC 2
+#define GTK_VARIANT_TENSOR_CORE 3
+int gtk_set_kernel_variant(gtk_tensor *t, int variant);
+int gtk_get_kernel_variant(const gtk_tensor *t, int *variant);
+int gtk_autotune(gtk_tensor *t, int *variant);
+/* A batch of handles on one device swept together: gtk_batch_sweep runs one
+ * sweep (gtk_sweep) of every handle -- the first eagerly, later ones as one
+ * replayed CUDA graph whose per-handle branches run concurrently -- and writes
+ * fits[i] for handle i.  Handles keep their own state and may also be used on
+ * their own between batch sweeps (not concurrently with one); a change of a
+ * handle's precision or variant recaptures the graph.  Destroy the batch before
+ * its handles.  gtk_batch_kernels: kernels in one replay of the graph (0 before
+ * the first capture). */
+typedef struct gtk_batch gtk_batch;
+int gtk_batch_create(gtk_tensor *const *tensors, int count, gtk_batch **out);
+int gtk_batch_sweep(gtk_batch *b, double *fits);
+int gtk_batch_kernels(const gtk_batch *b, uint64_t *kernels);
+void gtk_batch_destroy(gtk_batch *b);
+
 /* ---- no device allocation ----------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory where they run -- work recorded into a CUDA graph by stream capture,
