@@ -26,7 +26,7 @@ fit after the K sweeps is within 1e-4 of the plain form's, else the plain form's
                  run the configuration's 10 sweeps with a fit each, read the
                  factors back -- N * nnz * sweeps / wall time.
   roofline ..... the dominant kernel (fused delta + Gram/RHS) of the chosen form:
-                 SURVEY's compulsory delta bytes (4N + 4J per nonzero and mode)
+                 the compulsory bytes of the unfused delta (4N + 4J per nonzero and mode)
                  per launch over its event-timed duration, against the measured
                  HBM copy bandwidth; tensor or FP32 throughput beside it.
   cpu_baseline . the CPU restatement of the reference (its OpenMP delta/B,C/LU
@@ -436,7 +436,7 @@ def main():
         "traffic": traffic,
         "kernel": ("k_mode_spec<float,4,10,2,kUpdate>" if chosen == "plain"
                    else f"k_mode_tc<10,3,{chosen},update>") + " (fused delta + Gram/RHS)",
-        "bytes_per_launch": bytes_per_launch, "bytes_note": "SURVEY B_delta = 4N + 4J bytes per nonzero and mode",
+        "bytes_per_launch": bytes_per_launch, "bytes_note": "unfused delta: B_delta = 4N + 4J bytes per nonzero and mode",
         "launch_ms": per_launch_s * 1e3, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
     } | compute
     kernels = {name: {"launches": n, "ms_per_launch": m / max(1, n)} for name, (m, n) in r["kernels"].items()}

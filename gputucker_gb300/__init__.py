@@ -10,6 +10,9 @@ from .tucker import (  # noqa: F401
     Batch,
     BlockedTensor,
     Coo,
+    checkpoint_info,
+    device_memory,
+    plan_partition,
     coo_from_arrays,
     create_tensor_blocks,
     generate,
@@ -17,9 +20,12 @@ from .tucker import (  # noqa: F401
     parse_buffer,
     parse_from_file,
     tucker_decomposition,
+    WarmStart,
+    ws_features,
 )
 
 __all__ = [
-    "GTKError", "LIB_PATH", "Batch", "BlockedTensor", "Coo", "coo_from_arrays", "create_tensor_blocks", "generate",
-    "generate_planted", "parse_buffer", "parse_from_file", "tucker_decomposition",
+    "GTKError", "LIB_PATH", "Batch", "BlockedTensor", "Coo", "checkpoint_info", "coo_from_arrays",
+    "create_tensor_blocks", "device_memory", "generate", "generate_planted", "parse_buffer", "parse_from_file",
+    "plan_partition", "tucker_decomposition", "WarmStart", "ws_features",
 ]

@@ -61,6 +61,14 @@ class TensorInfo(C.Structure):
     ]
 
 
+class Plan(C.Structure):
+    _fields_ = [
+        ("partition_dims", C.c_uint32 * GTK_MAX_ORDER), ("block_dims", C.c_uint32 * GTK_MAX_ORDER),
+        ("block_count", C.c_uint64), ("dimension_based", C.c_int), ("streams", C.c_int),
+        ("avail_nnz_per_task", C.c_uint64), ("required_bytes", C.c_uint64), ("block_bytes", C.c_uint64),
+    ]
+
+
 P = C.c_void_p
 U32P = C.POINTER(C.c_uint32)
 U64P = C.POINTER(C.c_uint64)
@@ -102,6 +110,24 @@ SIGNATURES = {
     "gtk_write_text": (C.c_int, [P, C.c_char_p]),
     "gtk_reconstruction_error_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_uint64, C.POINTER(P), P, C.POINTER(P), P, P,
                                                    P]),
+    "gtk_plan_partition": (C.c_int, [C.c_int, U32P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_uint64,
+                                     C.POINTER(Plan)]),
+    "gtk_device_memory": (C.c_int, [C.c_int, U64P, U64P]),
+    "gtk_checkpoint_save": (C.c_int, [P, C.c_char_p, C.POINTER(C.c_double), C.c_int]),
+    "gtk_checkpoint_load": (C.c_int, [P, C.c_char_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int)]),
+    "gtk_checkpoint_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), U32P,
+                                      U32P, C.POINTER(C.c_int)]),
+    "gtk_ws_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int, C.POINTER(P)]),
+    "gtk_ws_destroy": (None, [P]),
+    "gtk_ws_info": (C.c_int, [P, C.POINTER(C.c_int), U64P, U64P]),
+    "gtk_ws_get_params": (C.c_int, [P, P, P, P]),
+    "gtk_ws_set_params": (C.c_int, [P, P, P, P]),
+    "gtk_ws_features": (C.c_int, [P, C.c_int, P]),
+    "gtk_ws_add_example": (C.c_int, [P, P]),
+    "gtk_ws_train": (C.c_int, [P, C.c_int, C.c_int, C.c_float, C.POINTER(C.c_double)]),
+    "gtk_ws_apply": (C.c_int, [P, P]),
+    "gtk_ws_loss_grad": (C.c_int, [P, P, P, C.c_int, C.POINTER(C.c_double), P]),
+    "gtk_ws_predict": (C.c_int, [P, P, C.c_int, P]),
     "gtk_set_kernel_variant": (C.c_int, [P, C.c_int]),
     "gtk_get_kernel_variant": (C.c_int, [P, C.POINTER(C.c_int)]),
     "gtk_autotune": (C.c_int, [P, C.POINTER(C.c_int)]),

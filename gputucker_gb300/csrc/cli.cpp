@@ -8,7 +8,11 @@
 // reference's stopping threshold, tucker.cuh:183), --seed (glibc srand seed,
 // default 1 = the reference's unseeded rand()), --dtype f32|f64 (main.cu:25
 // uses double), --device, --write-factors PREFIX (factor n in the slab layout,
-// one text row per factor row).
+// one text row per factor row), --checkpoint PATH (factors, core and fits saved
+// after every sweep), --resume PATH (start from a saved checkpoint: its factors
+// and core, sweep count and last fit).  Without -p the partition comes from the
+// planner (gtk_plan_partition) with the device's free memory, as the
+// reference's TuckerDecomposition does (tucker.cuh:49-55).
 
 #include <sys/stat.h>
 
@@ -29,13 +33,15 @@ static void usage() {
       "  -o [ --order ] arg     Order\n"
       "  -r [ --rank ] arg (=10)  Rank\n"
       "  -g [ --gpus ] arg (=1)   The number of GPUs (this build: 1)\n"
-      "  -p [ --partition ] P1,..,PN (=1,..,1)  Partition parameters\n"
+      "  -p [ --partition ] P1,..,PN (=planned)  Partition parameters\n"
       "  --iters arg (=3)       Maximum ALS sweeps\n"
       "  --tol arg (=1e-4)      Stop when |fit - previous fit| <= tol\n"
       "  --seed arg (=1)        glibc srand() seed of the initialisation\n"
       "  --dtype f32|f64 (=f64) Value type\n"
       "  --device arg (=0)      CUDA device\n"
-      "  --write-factors PREFIX Write PREFIX<n>.txt per factor\n");
+      "  --write-factors PREFIX Write PREFIX<n>.txt per factor\n"
+      "  --checkpoint PATH      Save factors, core and fits after every sweep\n"
+      "  --resume PATH          Continue from a checkpoint\n");
 }
 
 static double now() {
@@ -52,7 +58,7 @@ static double now() {
   } while (0)
 
 int main(int argc, char **argv) {
-  std::string input, prefix, parts;
+  std::string input, prefix, parts, ckpt, resume;
   int order = -1, rank = 10, gpus = 1, iters = 3, dtype = GTK_F64, device = 0;
   double tol = 1e-4;
   unsigned seed = 1;
@@ -96,6 +102,10 @@ int main(int argc, char **argv) {
       device = atoi(val("device"));
     } else if (a == "--write-factors") {
       prefix = val("write-factors");
+    } else if (a == "--checkpoint") {
+      ckpt = val("checkpoint");
+    } else if (a == "--resume") {
+      resume = val("resume");
     } else {
       fprintf(stderr, "[ERROR] Parsing error : unrecognised option '%s'\n", a.c_str());
       usage();
@@ -153,6 +163,14 @@ int main(int argc, char **argv) {
   printf("Parse time : %lf\n", now() - t0);
   for (int n = 0; n < order; ++n) printf("Max. dim[%d] = %u\n", n, dims[n]);
   printf("# nnzs: %llu\n", (unsigned long long)nnz);
+  if (parts.empty()) {
+    uint64_t free_b = 0, total_b = 0;
+    CHECK(gtk_device_memory(device, &free_b, &total_b));
+    gtk_plan plan;
+    CHECK(gtk_plan_partition(order, dims.data(), nnz, rank, dtype, 1, free_b, &plan));
+    for (int n = 0; n < order; ++n) P[n] = plan.partition_dims[n];
+    printf("Partitioning Type: %s\n", plan.dimension_based ? "Dimension-based" : "Nonzero-based");
+  }
   t0 = now();
   gtk_tensor *t = nullptr;
   CHECK(gtk_create_blocks(coo, P.data(), rank, device, &t));
@@ -165,8 +183,20 @@ int main(int argc, char **argv) {
   CHECK(gtk_init_random(t, seed, draws));
   double p_fit = -1, fit = -1;
   int it = 0;
+  std::vector<double> fits;
+  if (!resume.empty()) {
+    std::vector<double> saved(4096);
+    int nsaved = 0;
+    CHECK(gtk_checkpoint_load(t, resume.c_str(), saved.data(), (int)saved.size(), &nsaved));
+    const int k = nsaved < (int)saved.size() ? nsaved : (int)saved.size();
+    fits.assign(saved.begin(), saved.begin() + k);
+    it = nsaved;
+    if (k > 0) p_fit = fits.back();
+    printf("Resumed from %s after %d sweeps (fit %lf)\n", resume.c_str(), it, p_fit);
+  }
+  const int it0 = it;
   double avg = now();
-  while (true) {
+  while (it < iters) {
     double itertime = now(), step = itertime;
     CHECK(gtk_update_factor_matrices(t));
     CHECK(gtk_synchronize(t));
@@ -175,12 +205,14 @@ int main(int argc, char **argv) {
     CHECK(gtk_reconstruction(t, &fit));
     printf("Recon Time : %lf\n\n", now() - step);
     ++it;
+    fits.push_back(fit);
+    if (!ckpt.empty()) CHECK(gtk_checkpoint_save(t, ckpt.c_str(), fits.data(), (int)fits.size()));
     printf("iter %d\t Fit: %.10g\n", it, fit);
     printf("iter%d :      Fit : %lf\tElapsed Time : %lf\n\n", it, fit, now() - itertime);
     if (it >= iters || (p_fit != -1 && (p_fit - fit > 0 ? p_fit - fit : fit - p_fit) <= tol)) break;
     p_fit = fit;
   }
-  printf("Average sweep time : %lf\n", (now() - avg) / it);
+  printf("Average sweep time : %lf\n", (now() - avg) / (it - it0 > 0 ? it - it0 : 1));
   if (!prefix.empty()) {
     for (int n = 0; n < order; ++n) {
       const size_t rows = (size_t)P[n] * info.block_dims[n];

@@ -256,6 +256,20 @@ class BlockedTensor:
     def set_graph(self, on: bool = True) -> None:
         call("gtk_set_graph", self.handle, 1 if on else 0)
 
+    # ---- checkpoint
+    def checkpoint_save(self, path: str, fits=()) -> None:
+        """Factors, core and fit history to `path` (gtk_checkpoint_save)."""
+        f = (C.c_double * max(1, len(fits)))(*fits)
+        call("gtk_checkpoint_save", self.handle, str(path).encode(), f, len(fits))
+
+    def checkpoint_load(self, path: str, fits_cap: int = 1024) -> list:
+        """Restore factors and core from `path`; returns the saved fit history."""
+        f = (C.c_double * max(1, fits_cap))()
+        n = C.c_int()
+        call("gtk_checkpoint_load", self.handle, str(path).encode(), f, fits_cap, C.byref(n))
+        k = min(n.value, fits_cap)
+        return [f[i] for i in range(k)]
+
     VARIANTS = {"auto": -1, "simt2": 0, "simt1": 1, "generic": 2, "tensor_core": 3}
 
     def set_kernel_variant(self, variant: str) -> None:
@@ -365,6 +379,126 @@ class Batch:
             pass
 
 
+def plan_partition(dims, nnz: int, rank: int, dtype="f32", gpu_count: int = 1, gpu_mem_bytes: int | None = None,
+                   device: int = 0) -> dict:
+    """Optimizer::FindPartitionParms (optimizer.tpp:71-89): P_n for a tensor of this size on
+    gpu_count GPUs of gpu_mem_bytes each (default: the free memory of `device`)."""
+    if gpu_mem_bytes is None:
+        gpu_mem_bytes = device_memory(device)[0]
+    d = np.ascontiguousarray(dims, dtype=np.uint32)
+    plan = nat.Plan()
+    call("gtk_plan_partition", len(d), d.ctypes.data_as(nat.U32P), nnz, rank, _dtype_code(dtype), gpu_count,
+         gpu_mem_bytes, C.byref(plan))
+    N = len(d)
+    return dict(partition_dims=list(plan.partition_dims[:N]), block_dims=list(plan.block_dims[:N]),
+                block_count=plan.block_count, dimension_based=bool(plan.dimension_based), streams=plan.streams,
+                avail_nnz_per_task=plan.avail_nnz_per_task, required_bytes=plan.required_bytes,
+                block_bytes=plan.block_bytes)
+
+
+def device_memory(device: int = 0) -> tuple[int, int]:
+    """(free, total) bytes of a device (cudaMemGetInfo)."""
+    f, t = C.c_uint64(), C.c_uint64()
+    call("gtk_device_memory", device, C.byref(f), C.byref(t))
+    return f.value, t.value
+
+
+def checkpoint_info(path: str) -> dict:
+    """Header of a checkpoint file (no device needed)."""
+    o, r, d, nf = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    dims = (C.c_uint32 * nat.GTK_MAX_ORDER)()
+    P = (C.c_uint32 * nat.GTK_MAX_ORDER)()
+    call("gtk_checkpoint_info", str(path).encode(), C.byref(o), C.byref(r), C.byref(d), dims, P, C.byref(nf))
+    return dict(order=o.value, rank=r.value, dtype="f64" if d.value == nat.GTK_F64 else "f32",
+                dims=list(dims[:o.value]), partition_dims=list(P[:o.value]), nfits=nf.value)
+
+
+class WarmStart:
+    """Learned warm start (gtk_ws_*): an MLP from per-row statistics to initial factor rows,
+    trained and run by the library's CUDA kernels.  Uniform [0,1) init stays the fallback."""
+
+    def __init__(self, order: int, rank: int, hidden: int = 64, seed: int = 0, device: int = 0):
+        h = C.c_void_p()
+        call("gtk_ws_create", order, rank, hidden, seed, device, C.byref(h))
+        self._h = h
+        self.order, self.rank, self.hidden = order, rank, hidden
+        f, n = C.c_int(), C.c_uint64()
+        call("gtk_ws_info", h, C.byref(f), C.byref(n), None)
+        self.features, self.n_params = f.value, n.value
+
+    @property
+    def handle(self):
+        if self._h is None:
+            raise ValueError("warm-start model is closed")
+        return self._h
+
+    def examples(self) -> int:
+        n = C.c_uint64()
+        call("gtk_ws_info", self.handle, None, None, C.byref(n))
+        return n.value
+
+    def add_example(self, t: BlockedTensor) -> None:
+        call("gtk_ws_add_example", self.handle, t.handle)
+
+    def train(self, steps: int, batch: int = 1024, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        call("gtk_ws_train", self.handle, steps, batch, lr, C.byref(loss))
+        return loss.value
+
+    def apply(self, t: BlockedTensor) -> None:
+        call("gtk_ws_apply", self.handle, t.handle)
+
+    def get_params(self):
+        p = np.empty(self.n_params, np.float32)
+        mu = np.empty(self.features, np.float32)
+        sd = np.empty(self.features, np.float32)
+        call("gtk_ws_get_params", self.handle, _ptr(p), _ptr(mu), _ptr(sd))
+        return p, mu, sd
+
+    def set_params(self, params=None, feat_mean=None, feat_std=None) -> None:
+        arrs = [None if a is None else np.ascontiguousarray(a, np.float32) for a in (params, feat_mean, feat_std)]
+        call("gtk_ws_set_params", self.handle, *[None if a is None else _ptr(a) for a in arrs])
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, np.float32)
+        t = np.ascontiguousarray(t, np.float32)
+        g = np.empty(self.n_params, np.float32)
+        loss = C.c_double()
+        call("gtk_ws_loss_grad", self.handle, _ptr(x), _ptr(t), x.shape[0], C.byref(loss), _ptr(g))
+        return loss.value, g
+
+    def predict(self, x):
+        x = np.ascontiguousarray(x, np.float32)
+        y = np.empty((x.shape[0], self.rank), np.float32)
+        call("gtk_ws_predict", self.handle, _ptr(x), x.shape[0], _ptr(y))
+        return y
+
+    def close(self) -> None:
+        if self._h is not None:
+            nat.load().gtk_ws_destroy(self._h)
+            self._h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ws_features(t: BlockedTensor, mode: int) -> np.ndarray:
+    """Raw warm-start features of every row of `mode` (rows x F)."""
+    F = 3 + 3 * (t.order - 1) + t.order
+    out = np.empty((t.factor_rows(mode), F), np.float32)
+    call("gtk_ws_features", t.handle, mode, _ptr(out))
+    return out
+
+
 def create_tensor_blocks(coo: Coo, partition_dims, rank: int, device: int = 0) -> BlockedTensor:
     """CreateTensorBlocks + AssignIndicesOfEachBlock on the GPU (gtk_create_blocks)."""
     P = np.ascontiguousarray(partition_dims, dtype=np.uint32)
@@ -380,7 +514,8 @@ def tucker_decomposition(coo: Coo, rank: int, partition_dims=None, max_iters: in
     """TuckerDecomposition (tucker.cuh:30-190): blocks, init from the glibc stream that
     continues after the parser's draws, then sweeps until max_iters or |dfit| <= tol.
     Returns (tensor, fits)."""
-    P = partition_dims or [1] * coo.order
-    t = create_tensor_blocks(coo, P, rank, device)
+    if partition_dims is None:  # the reference plans P_n from the GPU memory (tucker.cuh:49-55)
+        partition_dims = plan_partition(coo.dims, coo.nnz, rank, coo.dtype, 1, None, device)["partition_dims"]
+    t = create_tensor_blocks(coo, partition_dims, rank, device)
     t.init_random(rand_seed, coo.rand_draws)
     return t, t.tucker_decomposition(max_iters, tol)

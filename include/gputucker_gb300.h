@@ -163,6 +163,43 @@ int gtk_set_graph(gtk_tensor *t, int on);
  * delta.cuh:206).  A parity hook: the sweep itself never writes delta to HBM. */
 int gtk_compute_delta(gtk_tensor *t, int mode, void *delta);
 
+/* ---- partition planner --------------------------------------------------
+ * Replaces Optimizer::FindPartitionParms (optimizer.tpp:71-89), which
+ * TuckerDecomposition calls with the GPU memory it could allocate
+ * (tucker.cuh:49-55): same inputs, same P_n.  If the whole problem (tensor,
+ * delta, core and factors per GPU) fits gpu_count * gpu_mem_bytes the plan is
+ * "nonzero-based": P_n = 1.  Otherwise ("dimension-based") P_n grows on the mode
+ * with the largest block until one block's data fits a quarter of one GPU's
+ * memory and there are at least 4 blocks per GPU.  GTK_ERR_PARTITION where the
+ * reference throws (a P_n that would leave an empty last slab).
+ * gtk_device_memory reports cudaMemGetInfo of a device, the figure to plan with. */
+typedef struct gtk_plan {
+  uint32_t partition_dims[GTK_MAX_ORDER]; /* P_n */
+  uint32_t block_dims[GTK_MAX_ORDER];     /* ceil(dims[n] / P_n) */
+  uint64_t block_count;
+  int dimension_based;         /* 0: nonzero-based (fits), 1: dimension-based */
+  int streams;                 /* CUDA streams per GPU the reference would run: 1 or 4 */
+  uint64_t avail_nnz_per_task; /* the reference's per-task nonzero budget */
+  uint64_t required_bytes;     /* whole-problem bytes the decision compares with the GPUs' memory */
+  uint64_t block_bytes;        /* one block's data (GetAllDataSize) under the plan */
+} gtk_plan;
+int gtk_plan_partition(int order, const uint32_t *dims, uint64_t nnz, int rank, int dtype, int gpu_count,
+                       uint64_t gpu_mem_bytes, gtk_plan *out);
+int gtk_device_memory(int device, uint64_t *free_bytes, uint64_t *total_bytes);
+
+/* ---- checkpoint ---------------------------------------------------------
+ * No reference counterpart.  gtk_checkpoint_save writes the factors, the core
+ * and an optional fit history (fits[0..nfits)) of a handle to `path` (binary,
+ * FNV-1a checksum, written to path.tmp then renamed).  gtk_checkpoint_load
+ * restores them into a handle of the same shape, rank, value type and partition
+ * (else GTK_ERR_ARG; a damaged file is GTK_ERR_PARSE) and returns the last
+ * min(nfits, fits_cap) fits; sweeps then continue where the saved run stopped.
+ * gtk_checkpoint_info reads the header only (no device needed). */
+int gtk_checkpoint_save(gtk_tensor *t, const char *path, const double *fits, int nfits);
+int gtk_checkpoint_load(gtk_tensor *t, const char *path, double *fits, int fits_cap, int *nfits);
+int gtk_checkpoint_info(const char *path, int *order, int *rank, int *dtype, uint32_t *dims, uint32_t *partition_dims,
+                        int *nfits);
+
 /* ---- kernel variants, autotuner, batches -------------------------------
  * No reference counterpart.  The update kernel of a handle is one of:
  * GTK_VARIANT_SIMT2 / SIMT1 (specialised SIMT kernels, 2 or 1 nonzeros per
@@ -195,6 +232,39 @@ int gtk_batch_create(gtk_tensor *const *tensors, int count, gtk_batch **out);
 int gtk_batch_sweep(gtk_batch *b, double *fits);
 int gtk_batch_kernels(const gtk_batch *b, uint64_t *kernels);
 void gtk_batch_destroy(gtk_batch *b);
+
+/* ---- learned warm start -------------------------------------------------
+ * No reference counterpart (the reference starts from uniform [0,1) draws,
+ * tucker.cuh:84-97, which stay the fallback).  A small MLP (two hidden ReLU
+ * layers of `hidden` units) maps per-row statistics of a tensor to initial
+ * factor rows.  Features of row i of mode n (F = 3 + 3(order-1) + order floats):
+ * log(1+c_i), mean and std of the row's values; for each other mode m, mean and
+ * std over the row's nonzeros of the co-indexed row's mean value, and mean of
+ * log(1 + its nonzero count); one-hot of n.  Training and inference run in the
+ * library's CUDA kernels (FP32, Adam).
+ *   gtk_ws_add_example: the handle's current factors (converged by the plain
+ *     method) become training targets for the features of its non-empty rows;
+ *   gtk_ws_train: `steps` Adam steps on random batches of the examples (the
+ *     feature standardisation is fixed from the examples at the first call);
+ *   gtk_ws_apply: writes predicted factor rows into every mode of a handle whose
+ *     core is set (gtk_init_random first: its core is kept, its factors replaced;
+ *     padding rows 0);
+ *   gtk_ws_loss_grad / gtk_ws_predict: one forward (+ backward) pass on host
+ *     arrays of already standardised features (gradient checks, inspection);
+ *     grad receives the flat parameter gradient in gtk_ws_get_params order:
+ *     W1 [hidden x F], b1, W2 [hidden x hidden], b2, W3 [rank x hidden], b3. */
+typedef struct gtk_ws gtk_ws;
+int gtk_ws_create(int order, int rank, int hidden, uint64_t seed, int device, gtk_ws **out);
+void gtk_ws_destroy(gtk_ws *m);
+int gtk_ws_info(const gtk_ws *m, int *features, uint64_t *params, uint64_t *examples);
+int gtk_ws_get_params(const gtk_ws *m, float *params, float *feat_mean, float *feat_std);
+int gtk_ws_set_params(gtk_ws *m, const float *params, const float *feat_mean, const float *feat_std);
+int gtk_ws_features(gtk_tensor *t, int mode, float *out);  /* raw features, rows of mode x F, host */
+int gtk_ws_add_example(gtk_ws *m, gtk_tensor *t);
+int gtk_ws_train(gtk_ws *m, int steps, int batch, float lr, double *final_loss);
+int gtk_ws_apply(gtk_ws *m, gtk_tensor *t);
+int gtk_ws_loss_grad(gtk_ws *m, const float *x, const float *target, int batch, double *loss, float *grad);
+int gtk_ws_predict(gtk_ws *m, const float *x, int batch, float *y);
 
 /* ---- no device allocation ----------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

@@ -217,7 +217,45 @@ template <class V> double do_fit(Ref<V> &r, double *err_out) {
     else { auto &r = (h)->d; expr; }                       \
   } while (0)
 
+namespace {
+
+// Optimizer::FindPartitionParms (optimizer.tpp:71-89) on a tensor that has only
+// order, dims and nnz_count set -- all the planner reads.
+template <class V>
+int do_plan(int order, const uint32_t *dims, uint64_t nnz, int J, int gpus, uint64_t mem, uint32_t *P, uint32_t *bd,
+            uint64_t *info) {
+  using tensor_t = typename Ref<V>::tensor_t;
+  try {
+    tensor_t *t = new tensor_t((unsigned short)order);
+    for (int n = 0; n < order; ++n) t->dims[n] = dims[n];
+    t->nnz_count = nnz;
+    Optimizer<tensor_t> *opt = new Optimizer<tensor_t>();
+    opt->Initialize((unsigned short)gpus, (unsigned)J, mem, t);
+    uint32_t *pd = opt->FindPartitionParms();
+    for (int n = 0; n < order; ++n) {
+      P[n] = pd[n];
+      bd[n] = opt->block_dims[n];
+    }
+    info[0] = opt->block_count;
+    info[1] = opt->partition_type == enums::PartitionTypes::kDimensionPartition ? 1 : 0;
+    info[2] = (uint64_t)opt->cuda_stream_count;
+    info[3] = opt->avail_nnz_count_per_task;
+  } catch (std::exception &e) {
+    g_err = e.what();
+    return 3;
+  }
+  return 0;
+}
+
+}  // namespace
+
 extern "C" {
+
+int ref_plan(int order, const uint32_t *dims, uint64_t nnz, int J, int dtype, int gpus, uint64_t mem, uint32_t *P,
+             uint32_t *bd, uint64_t *info) {
+  return dtype == 1 ? do_plan<double>(order, dims, nnz, J, gpus, mem, P, bd, info)
+                    : do_plan<float>(order, dims, nnz, J, gpus, mem, P, bd, info);
+}
 
 const char *ref_last_error(void) { return g_err.c_str(); }
 

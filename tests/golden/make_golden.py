@@ -12,7 +12,10 @@ input text file (<case>.tns) and <case>.npz holding:
   delta0_<n>                                                   delta of mode n, initial factors
   fac<s+1>_<n>, fit<s+1>                                       factors and fit after sweep s
 
-Usage (needs the reference sources): python tests/golden/make_golden.py
+It also writes planner_cases.json: Optimizer::FindPartitionParms of the
+reference (optimizer.tpp:71-89) on the shapes and memory sizes of PLANNER_CASES.
+
+Usage (needs the reference sources): python tests/golden/make_golden.py [--planner-only]
 """
 
 from __future__ import annotations
@@ -87,8 +90,45 @@ def make(case):
     print(name, "nnz", r.nnz, "blocks", r.nblk, "fits", [float(out[f"fit{s + 1}"]) for s in range(SWEEPS)])
 
 
+# partition planner cases: dims, nnz, rank, dtype, gpus, GPU memory bytes
+GB = 1 << 30
+PLANNER_CASES = [
+    ([10_000] * 3, 1_000_000, 10, 1, 1, 280 * GB),             # uniform 3-order, 1M nonzeros (fits)
+    ([100_000] * 4, 100_000_000, 10, 0, 1, 280 * GB),          # 4-order Zipf, 100M nonzeros (fits)
+    ([1_000_000] * 3, 500_000_000, 16, 0, 1, 280 * GB),        # 3-order, 500M nonzeros (fits)
+    ([50_000] * 3, 20_000_000, 8, 0, 1, 280 * GB),             # planted 3-order, 20M observed
+    ([100_000] * 4, 100_000_000, 10, 0, 1, 4 * GB),            # does not fit: dimension-based
+    ([100_000] * 4, 100_000_000, 10, 0, 4, 4 * GB),
+    ([1_000_000] * 3, 500_000_000, 16, 0, 1, 16 * GB),
+    ([1_000_000] * 3, 500_000_000, 16, 1, 2, 24 * GB),
+    ([37, 12_345, 999_999], 3_000_000, 8, 1, 1, 256 << 20),
+    ([5, 7, 3, 11], 300, 4, 1, 1, 1 << 16),                   # tiny memory: P grows until a slab is empty
+    ([1000, 2000, 3000, 4000, 5000], 10_000_000, 4, 0, 3, 1 * GB),
+    ([123_456, 654_321], 50_000_000, 32, 1, 1, 2 * GB),
+    ([2**20, 3, 2**20], 80_000_000, 12, 0, 1, 3 * GB),
+    ([10] * 8, 90_000, 2, 1, 1, 1 << 20),
+    ([3, 3, 3], 27, 4, 1, 1, 1000),                            # never fits: the reference throws
+    ([10, 10], 100, 2, 0, 1, 600),                             # P = 6 of dim 10 leaves an empty slab
+]
+
+
+def make_planner():
+    import json
+    from oracle_util import ref_plan
+    out = []
+    for dims, nnz, J, dt, gpus, mem in PLANNER_CASES:
+        st, P, bd, nblk, dim_based, streams, avail = ref_plan(dims, nnz, J, dt, gpus, mem)
+        out.append(dict(dims=dims, nnz=nnz, rank=J, dtype=dt, gpus=gpus, mem=mem, status=st, P=P, block_dims=bd,
+                        block_count=nblk, dimension_based=dim_based, streams=streams, avail_nnz_per_task=avail))
+        print("planner", dims, nnz, J, dt, gpus, mem, "->", st, P, nblk, dim_based)
+    with open(os.path.join(HERE, "planner_cases.json"), "w") as f:
+        json.dump(out, f, indent=1)
+
+
 if __name__ == "__main__":
     if not ref_available():
         sys.exit("oracle/_ref/libgtk_ref.so is missing: build it with `make -C oracle ref`")
-    for c in CASES:
-        make(c)
+    if "--planner-only" not in sys.argv:
+        for c in CASES:
+            make(c)
+    make_planner()

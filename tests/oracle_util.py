@@ -88,6 +88,8 @@ def ref_lib():
         lib.ref_fit.argtypes = [C.c_void_p, C.c_void_p]
         lib.ref_fit.restype = C.c_double
         lib.ref_last_error.restype = C.c_char_p
+        lib.ref_plan.argtypes = [C.c_int, C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_void_p,
+                                 C.c_void_p, C.c_void_p]
         _ref = lib
     return _ref
 
@@ -328,3 +330,26 @@ def rel_fro(a, b):
     b = np.asarray(b, np.float64)
     nb = np.linalg.norm(b)
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+def ref_plan(dims, nnz, rank, dtype, gpus, mem):
+    """Optimizer::FindPartitionParms of the reference (optimizer.tpp:71-89), compiled in
+    place: (status, P, block_dims, block_count, dimension_based, streams, avail_nnz_per_task)."""
+    N = len(dims)
+    d = np.ascontiguousarray(dims, dtype=np.uint32)
+    P = np.zeros(N, np.uint32)
+    bd = np.zeros(N, np.uint32)
+    info = np.zeros(4, np.uint64)
+    st = ref_lib().ref_plan(N, d.ctypes.data, nnz, rank, dtype, gpus, mem, P.ctypes.data, bd.ctypes.data,
+                            info.ctypes.data)
+    return st, P.tolist(), bd.tolist(), int(info[0]), int(info[1]), int(info[2]), int(info[3])
+
+
+def ws_oracle():
+    """oracle/warmstart_oracle.py (the warm start's CPU restatement)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("warmstart_oracle", os.path.join(ROOT, "oracle",
+                                                                                   "warmstart_oracle.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod

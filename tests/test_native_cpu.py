@@ -196,3 +196,68 @@ def test_cli_usage(native):
     assert r.returncode == 2 and "Input file must be specified" in r.stdout
     r = subprocess.run([cli, "-i", "/nonexistent", "-o", "3"], capture_output=True, text=True)
     assert r.returncode == 2
+
+
+# ---- partition planner (Optimizer::FindPartitionParms, optimizer.tpp:71-89)
+def _plan(native, dims, nnz, rank, dtype, gpus, mem):
+    plan = nat.Plan()
+    d = np.ascontiguousarray(dims, dtype=np.uint32)
+    rc = native.gtk_plan_partition(len(dims), d.ctypes.data_as(nat.U32P), nnz, rank, dtype, gpus, mem,
+                                   C.byref(plan))
+    N = len(dims)
+    return rc, list(plan.partition_dims[:N]), list(plan.block_dims[:N]), plan
+
+
+def test_planner_matches_reference_golden(native):
+    """Every case of planner_cases.json (produced by the reference's own optimizer)."""
+    import json
+    cases = json.load(open(os.path.join(ROOT, "tests", "golden", "planner_cases.json")))
+    assert len(cases) >= 15
+    for c in cases:
+        rc, P, bd, plan = _plan(native, c["dims"], c["nnz"], c["rank"], c["dtype"], c["gpus"], c["mem"])
+        if c["status"] != 0:  # the reference threw
+            assert rc == nat.GTK_ERR_PARTITION, c
+            continue
+        assert rc == 0, (c, native.gtk_last_error())
+        assert P == c["P"] and bd == c["block_dims"], c
+        assert plan.block_count == c["block_count"] and plan.dimension_based == c["dimension_based"], c
+        assert plan.streams == c["streams"] and plan.avail_nnz_per_task == c["avail_nnz_per_task"], c
+
+
+def test_planner_matches_reference_random(native):
+    """Random shapes and memory sizes against the reference compiled in place (when built)."""
+    from oracle_util import ref_available, ref_plan
+    if not ref_available():
+        pytest.skip("oracle/_ref not built")
+    rng = np.random.default_rng(5)
+    for _ in range(300):
+        N = int(rng.integers(1, 9))
+        dims = [int(x) for x in np.exp(rng.uniform(0, np.log(3e6), N)).astype(np.int64) + 1]
+        nnz = int(np.exp(rng.uniform(0, np.log(2e9))))
+        J = int(rng.integers(1, 33))
+        dt = int(rng.integers(0, 2))
+        gpus = int(rng.integers(1, 9))
+        mem = int(np.exp(rng.uniform(np.log(1e4), np.log(3e11))))
+        st, P, bd, nblk, dim_based, streams, avail = ref_plan(dims, nnz, J, dt, gpus, mem)
+        rc, P2, bd2, plan = _plan(native, dims, nnz, J, dt, gpus, mem)
+        if st != 0:
+            assert rc == nat.GTK_ERR_PARTITION
+            continue
+        assert rc == 0 and P2 == P and bd2 == bd, (dims, nnz, J, dt, gpus, mem, P, P2)
+        assert (plan.block_count, plan.dimension_based, plan.streams, plan.avail_nnz_per_task) == \
+            (nblk, dim_based, streams, avail)
+
+
+def test_planner_rejects_bad_arguments(native):
+    assert _plan(native, [10, 0], 5, 4, 0, 1, 1 << 30)[0] == nat.GTK_ERR_ARG
+    assert _plan(native, [10, 10], 5, 0, 0, 1, 1 << 30)[0] == nat.GTK_ERR_ARG
+    assert _plan(native, [10, 10], 5, 4, 7, 1, 1 << 30)[0] == nat.GTK_ERR_ARG
+    assert _plan(native, [10, 10], 5, 4, 0, 0, 1 << 30)[0] == nat.GTK_ERR_ARG
+
+
+def test_checkpoint_info_rejects_garbage(native, tmp_path):
+    p = tmp_path / "x.ckpt"
+    p.write_bytes(b"definitely not a checkpoint file")
+    assert native.gtk_checkpoint_info(str(p).encode(), None, None, None, None, None, None) == nat.GTK_ERR_PARSE
+    assert native.gtk_checkpoint_info(str(tmp_path / "missing").encode(), None, None, None, None, None,
+                                      None) == nat.GTK_ERR_IO

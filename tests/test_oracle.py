@@ -199,3 +199,36 @@ def test_oracle_fp32_vs_fp64_gap():
     # fit agrees to 1e-4: factor parity in FP32 is only meaningful on well-posed rows.
     gaps = [rel_fro(o32.get_factor(n), o64.get_factor(n)) for n in range(4)]
     assert max(gaps) < 5e-2
+
+
+def test_warmstart_oracle_gradient_finite_differences():
+    """The warm-start oracle's backward pass against central differences (float64)."""
+    from oracle_util import ws_oracle
+    orc = ws_oracle()
+    rng = np.random.default_rng(2)
+    F, H, J, B = 12, 7, 4, 9
+    n = H * F + H + H * H + H + J * H + J
+    p = rng.standard_normal(n) * 0.5
+    x = rng.standard_normal((B, F))
+    t = rng.standard_normal((B, J))
+    _, g = orc.loss_grad(p, x, t, F, H, J)
+    eps = 1e-6
+    num = np.empty(n)
+    for k in range(n):
+        e = np.zeros(n)
+        e[k] = eps
+        num[k] = (orc.loss_grad(p + e, x, t, F, H, J)[0] - orc.loss_grad(p - e, x, t, F, H, J)[0]) / (2 * eps)
+    assert np.abs(num - g).max() <= 1e-7 * max(1.0, np.abs(g).max())
+
+
+def test_warmstart_oracle_features_by_hand():
+    """3 nonzeros of a 2-order tensor, features written out by hand."""
+    from oracle_util import ws_oracle
+    orc = ws_oracle()
+    idx = [np.array([0, 0, 1]), np.array([1, 2, 2])]
+    vals = np.array([1.0, 3.0, 5.0])
+    f = orc.row_features(idx, vals, [2, 3], 0)
+    # row 0 of mode 0: c = 2, values 1, 3 -> mean 2, std 1; co-indexed mode-1 rows 1 (mean 1, c 1)
+    # and 2 (mean 4, c 2): mean 2.5, std 1.5, mean log1p(c) = (log 2 + log 3) / 2; one-hot [1, 0]
+    np.testing.assert_allclose(f[0], [np.log(3), 2, 1, 2.5, 1.5, (np.log(2) + np.log(3)) / 2, 1, 0])
+    np.testing.assert_allclose(f[1], [np.log(2), 5, 0, 4, 0, np.log(3), 1, 0])
