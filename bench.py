@@ -72,10 +72,14 @@ def args_parse():
     p.add_argument("--ref-sample", type=int, default=200_000, help="nonzeros per reference-arm step")
     p.add_argument("--precision", choices=["plain", "bf16", "tf32"], default="bf16",
                    help="tensor-core form timed beside plain FP32 (plain: only the plain form)")
-    p.add_argument("--workload", choices=["zipf4d_100M", "batch256"], default="zipf4d_100M",
-                   help="batch256: 256 independent tensors swept as one CUDA graph per sweep")
+    p.add_argument("--workload", choices=["zipf4d_100M", "batch256", "warmstart"], default="zipf4d_100M",
+                   help="batch256: 256 independent tensors swept as one CUDA graph per sweep; warmstart: the "
+                        "learned warm start on the planted 50,000^3 family")
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--batch-max-nnz", type=int, default=5_000_000, help="upper end of the per-tensor nnz range")
+    p.add_argument("--ws-train-seeds", type=int, default=24, help="training tensors of the warm-start family")
+    p.add_argument("--ws-held-seeds", type=int, default=6, help="held-out tensors of the warm-start family")
+    p.add_argument("--ws-nnz", type=int, default=20_000_000, help="observed entries per warm-start tensor")
     return p.parse_args()
 
 
@@ -336,11 +340,42 @@ def run_batch(args, dist):
             t.set_graph(False)
         res[form] = dict(wall=dist.max(wall), fits=fits, clocks=clk, kernels=kernels, solo=dist.max(solo), tc=tc,
                          tune_s=tune_s, variants={v: variants.count(v) for v in set(variants)})
-    for t in ts:
-        t.close()
     fast = forms[-1]
     gaps = np.abs(res[fast]["fits"] - res["plain"]["fits"])
     chosen = fast if float(gaps.max()) <= 1e-4 else "plain"
+    if chosen == "plain" and fast != "plain":
+        # per tensor: the precision form where its fit is within 1e-4 of plain FP32, else plain
+        for t, g in zip(ts, gaps):
+            t.init_random(1, 0)
+            t.set_kernel_variant("auto")
+            try:
+                t.set_precision(fast if g <= 1e-4 else "plain")
+            except gtk.GTKError:
+                t.set_precision("plain")
+            t.autotune()
+            t.init_random(1, 0)
+        with gtk.Batch(ts) as b:
+            for _ in range(max(2, args.warmup)):
+                b.sweep()
+            for t in ts:
+                t.init_random(1, 0)
+            clocks = Clocks(dist.local)
+            dist.barrier()
+            t0 = time.perf_counter()
+            fits = None
+            for _ in range(args.steps):
+                fits = b.sweep()
+            wall = time.perf_counter() - t0
+            dist.barrier()
+            clk = clocks.stop()
+            kernels = b.kernels()
+        mixed_gap = float(np.abs(fits - res["plain"]["fits"]).max())
+        res["mixed"] = dict(wall=dist.max(wall), fits=fits, clocks=clk, kernels=kernels, solo=None,
+                            tc=int(sum(g <= 1e-4 for g in gaps)), tune_s=0.0, variants={})
+        if mixed_gap <= 1e-4:
+            chosen = "mixed"
+    for t in ts:
+        t.close()
     r = res[chosen]
     if dist.rank == 0:
         line = {
@@ -357,16 +392,112 @@ def run_batch(args, dist):
                        "timing": "host wall clock per batch sweep (graph launch + fit read-back)",
                        "l2": "inputs (all tensors' views) exceed the 129 MB L2"},
             "forms": {f: {"nnz_per_s": work * args.steps / v["wall"], "ms_per_sweep": 1e3 * v["wall"] / args.steps,
-                          "one_by_one_ms_per_sweep": 1e3 * v["solo"], "batch_speedup_vs_one_by_one":
-                          v["solo"] / (v["wall"] / args.steps), "graph_kernels": v["kernels"],
+                          "one_by_one_ms_per_sweep": None if v["solo"] is None else 1e3 * v["solo"],
+                          "batch_speedup_vs_one_by_one":
+                          None if v["solo"] is None else v["solo"] / (v["wall"] / args.steps),
+                          "graph_kernels": v["kernels"],
                           "tensors_on_tensor_cores": v["tc"], "autotune_s": v["tune_s"], "variants": v["variants"]}
                       for f, v in res.items()},
-            "max_fit_gap_vs_plain": float(gaps.max()),
+            "max_fit_gap_vs_plain": float(np.abs(r["fits"] - res["plain"]["fits"]).max()),
+            "tensors_within_1e-4_in_precision_form": int(sum(g <= 1e-4 for g in gaps)),
             "speedup_vs_plain": res["plain"]["wall"] / r["wall"],
             "gpu_launches": r["kernels"] * args.steps,
             "clocks": r["clocks"],
         }
         print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ learned warm start
+WARM = dict(workload="warmstart_planted3d_50k", dims=[50_000] * 3, planted_rank=8, noise=0.01, rank=8,
+            sweeps_plain=10, converge_sweeps=30, train_steps=4000, batch=4096, lr=1e-3, hidden=64)
+
+
+def run_warmstart(args, dist):
+    """Planted 3-order family: train the warm-start MLP on the factors the plain
+    method converges to on the training seeds, then on held-out seeds count the
+    sweeps (and device time) the warm start needs to reach the plain method's fit
+    after 10 sweeps from uniform [0,1) init."""
+    import numpy as np
+
+    import gputucker_gb300 as gtk
+    W = WARM
+    J = W["rank"]
+
+    def tensor(seed):
+        coo = gtk.generate_planted(3, W["dims"], args.ws_nnz, W["planted_rank"], W["noise"], "f32", seed=seed)
+        return gtk.create_tensor_blocks(coo, [1, 1, 1], J, device=dist.local)
+
+    t0 = time.perf_counter()
+    ws = gtk.WarmStart(3, J, hidden=W["hidden"], seed=1, device=dist.local)
+    conv_sweeps = []
+    for s in range(args.ws_train_seeds):
+        with tensor(10_000 + s) as t:
+            t.init_random(1, 0)
+            t.set_graph(True)
+            prev = None
+            k = 0
+            for k in range(W["converge_sweeps"]):
+                f = t.sweep()
+                if prev is not None and abs(f - prev) <= 1e-6:
+                    break
+                prev = f
+            conv_sweeps.append(k + 1)
+            ws.add_example(t)
+    prep_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    loss = ws.train(W["train_steps"], W["batch"], W["lr"])
+    train_s = time.perf_counter() - t0
+    rows = []
+    for s in range(args.ws_held_seeds):
+        with tensor(20_000 + s) as t:
+            t.set_graph(True)
+            t.init_random(1, 0)
+            t.sweep()  # warm the graph
+            t.init_random(1, 0)
+            t.synchronize()
+            t.timer_begin()
+            plain = [t.sweep() for _ in range(W["sweeps_plain"])]
+            plain_ms = t.timer_end()
+            target = plain[-1]
+            t.init_random(1, 0)
+            t.synchronize()
+            a0 = time.perf_counter()
+            ws.apply(t)
+            apply_ms = 1e3 * (time.perf_counter() - a0)
+            t.timer_begin()
+            warm = []
+            while len(warm) < 2 * W["sweeps_plain"]:
+                warm.append(t.sweep())
+                if warm[-1] >= target:
+                    break
+            warm_ms = t.timer_end()
+        reached = warm[-1] >= target
+        # the reference's own loop stops after kMaxIteration = 3 sweeps (constants.hpp:17)
+        k3 = next((i + 1 for i, f in enumerate(warm) if f >= plain[2]), None)
+        rows.append(dict(plain_sweeps=W["sweeps_plain"], warm_sweeps=len(warm) if reached else None,
+                         warm_sweeps_to_plain3=k3, plain_ms=plain_ms, warm_ms=warm_ms + apply_ms, apply_ms=apply_ms,
+                         plain_fits=[round(x, 6) for x in plain], warm_fits=[round(x, 6) for x in warm]))
+    ws.close()
+    ok = [r for r in rows if r["warm_sweeps"] is not None]
+    ratio = (sum(r["warm_sweeps"] for r in ok) / sum(r["plain_sweeps"] for r in ok)) if ok else None
+    tratio = (sum(r["warm_ms"] for r in ok) / sum(r["plain_ms"] for r in ok)) if ok else None
+    ok3 = [r for r in rows if r["warm_sweeps_to_plain3"] is not None]
+    ratio3 = (sum(r["warm_sweeps_to_plain3"] for r in ok3) / (3 * len(ok3))) if ok3 else None
+    if dist.rank == 0:
+        print(json.dumps({
+            "metric": "learned warm start: sweeps to the plain method's 10-sweep fit, warm / plain",
+            "value": ratio, "unit": "ratio", "n_gpus": dist.world, "higher_is_better": False,
+            "time_ratio": tratio, "reached": f"{len(ok)}/{len(rows)}",
+            "ratio_vs_plain_3_sweeps": ratio3, "reached_3": f"{len(ok3)}/{len(rows)}",
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": W["workload"], "dims": W["dims"], "nnz": args.ws_nnz, "rank": J,
+                       "planted_rank": W["planted_rank"], "noise": W["noise"], "train_seeds": args.ws_train_seeds,
+                       "held_out_seeds": args.ws_held_seeds, "hidden": W["hidden"], "train_steps": W["train_steps"],
+                       "batch": W["batch"], "lr": W["lr"]},
+            "train": {"final_loss": loss, "prep_s": prep_s, "train_s": train_s, "examples_converge_sweeps":
+                      conv_sweeps},
+            "held_out": rows,
+        }), flush=True)
 
 
 def main():
@@ -379,6 +510,10 @@ def main():
         return
     if args.workload == "batch256":
         run_batch(args, dist)
+        dist.close()
+        return
+    if args.workload == "warmstart":
+        run_warmstart(args, dist)
         dist.close()
         return
     import gputucker_gb300 as gtk
@@ -413,12 +548,12 @@ def main():
     bytes_per_launch = nnz * (4 * N + 4 * J)
     achieved = bytes_per_launch / per_launch_s / 1e9
     traffic = None
-    try:
+    try:  # ncu capture of this kernel at the headline size, mean over the 4 mode launches
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             tr = json.load(f)
         key = "plain" if chosen == "plain" else "tc"
         if key in tr:
-            traffic = tr[key]["dram_bytes_per_nnz"] * nnz
+            traffic = tr[key]["mean_bytes_per_launch"] * nnz / tr["nnz"]
     except Exception:
         pass
     if chosen == "plain":

@@ -20,7 +20,9 @@
 //
 // Row statistics: the mode-m view is sorted by row, so a thread takes a
 // contiguous chunk of nonzeros, sums per row in registers and flushes with an
-// atomic add only when the row changes.
+// atomic add only when the row changes.  The sums are FP64: the standard
+// deviations come from E[a^2] - E[a]^2, which cancels in FP32 when the spread is
+// small against the mean (a one-time pass: the FP64 adds cost nothing visible).
 
 #include <cuda_runtime.h>
 
@@ -77,15 +79,15 @@ WsParams params_of(const gtk_ws *m, const float *w) {
 }
 
 // ---------------------------------------------------------------- row statistics
-// per row of the view: count, sum x, sum x^2 (FP32 sums of FP32/FP64 values)
+// per row of the view: count, sum x, sum x^2 (FP64 sums)
 template <class V>
 __global__ void k_row_stats(const uint32_t *__restrict__ row, const V *__restrict__ val, uint64_t nnz,
-                            float *__restrict__ cnt, float *__restrict__ s1, float *__restrict__ s2) {
+                            double *__restrict__ cnt, double *__restrict__ s1, double *__restrict__ s2) {
   const uint64_t t0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kChunk;
   if (t0 >= nnz) return;
   const uint64_t t1 = min(nnz, t0 + kChunk);
   uint32_t r = row[t0];
-  float c = 0.f, a = 0.f, b = 0.f;
+  double c = 0, a = 0, b = 0;
   for (uint64_t t = t0; t < t1; ++t) {
     const uint32_t rr = row[t];
     if (rr != r) {
@@ -93,10 +95,10 @@ __global__ void k_row_stats(const uint32_t *__restrict__ row, const V *__restric
       atomicAdd(s1 + r, a);
       atomicAdd(s2 + r, b);
       r = rr;
-      c = a = b = 0.f;
+      c = a = b = 0;
     }
-    const float x = (float)val[t];
-    c += 1.f;
+    const double x = (double)val[t];
+    c += 1;
     a += x;
     b += x * x;
   }
@@ -105,45 +107,45 @@ __global__ void k_row_stats(const uint32_t *__restrict__ row, const V *__restric
   atomicAdd(s2 + r, b);
 }
 
-// mu = sum / count, lc = log(1 + count), in place of s1 / s2
-__global__ void k_row_mean(const float *__restrict__ cnt, float *__restrict__ s1, float *__restrict__ lc,
-                           uint64_t rows) {
+// mu = sum / count, lc = log(1 + count) per row of a mode
+__global__ void k_row_mean(const double *__restrict__ cnt, const double *__restrict__ s1, double *__restrict__ mu,
+                           double *__restrict__ lc, uint64_t rows) {
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)gridDim.x * blockDim.x) {
-    const float c = cnt[r];
-    s1[r] = c > 0.f ? s1[r] / c : 0.f;
-    lc[r] = log1pf(c);
+    const double c = cnt[r];
+    mu[r] = c > 0 ? s1[r] / c : 0.0;
+    lc[r] = log1p(c);
   }
 }
 
 struct CoArgs {
   const uint32_t *row;             // view of mode n: global row of mode n
   const uint32_t *coord[kMaxOrder];  // view of mode n: coordinates of the other modes (compact, D entries)
-  const float *mu[kMaxOrder];
-  const float *lc[kMaxOrder];
+  const double *mu[kMaxOrder];
+  const double *lc[kMaxOrder];
   int D;
 };
 
 // per row of mode n, for each other mode: sum mu, sum mu^2, sum lc over the row's nonzeros
-__global__ void k_coindex(CoArgs a, uint64_t nnz, float *__restrict__ acc /* rows x 3D */) {
+__global__ void k_coindex(CoArgs a, uint64_t nnz, double *__restrict__ acc /* rows x 3D */) {
   const uint64_t t0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kChunk;
   if (t0 >= nnz) return;
   const uint64_t t1 = min(nnz, t0 + kChunk);
   const int D = a.D;
   uint32_t r = a.row[t0];
-  float s[3 * (kMaxOrder - 1)];
-  for (int k = 0; k < 3 * D; ++k) s[k] = 0.f;
+  double s[3 * (kMaxOrder - 1)];
+  for (int k = 0; k < 3 * D; ++k) s[k] = 0;
   for (uint64_t t = t0; t < t1; ++t) {
     const uint32_t rr = a.row[t];
     if (rr != r) {
       for (int k = 0; k < 3 * D; ++k) {
         atomicAdd(acc + (size_t)r * 3 * D + k, s[k]);
-        s[k] = 0.f;
+        s[k] = 0;
       }
       r = rr;
     }
     for (int d = 0; d < D; ++d) {
       const uint32_t c = a.coord[d][t];
-      const float m = a.mu[d][c];
+      const double m = a.mu[d][c];
       s[3 * d] += m;
       s[3 * d + 1] += m * m;
       s[3 * d + 2] += a.lc[d][c];
@@ -153,25 +155,25 @@ __global__ void k_coindex(CoArgs a, uint64_t nnz, float *__restrict__ acc /* row
 }
 
 // raw features of rows [0, rows) of mode n, F per row
-__global__ void k_features(const float *__restrict__ cnt, const float *__restrict__ s1, const float *__restrict__ s2,
-                           const float *__restrict__ acc, uint64_t rows, int N, int n, int F,
-                           float *__restrict__ out) {
+__global__ void k_features(const double *__restrict__ cnt, const double *__restrict__ s1,
+                           const double *__restrict__ s2, const double *__restrict__ acc, uint64_t rows, int N, int n,
+                           int F, float *__restrict__ out) {
   const int D = N - 1;
   for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)gridDim.x * blockDim.x) {
     float *o = out + r * F;
-    const float c = cnt[r];
-    const float inv = c > 0.f ? 1.f / c : 0.f;
-    const float mean = s1[r] * inv;  // s1 holds the raw sum here
-    const float var = fmaxf(0.f, s2[r] * inv - mean * mean);
-    o[0] = log1pf(c);
-    o[1] = mean;
-    o[2] = sqrtf(var);
+    const double c = cnt[r];
+    const double inv = c > 0 ? 1.0 / c : 0.0;
+    const double mean = s1[r] * inv;
+    const double var = fmax(0.0, s2[r] * inv - mean * mean);
+    o[0] = (float)log1p(c);
+    o[1] = (float)mean;
+    o[2] = (float)sqrt(var);
     for (int d = 0; d < D; ++d) {
-      const float *q = acc + r * 3 * D + 3 * d;
-      const float m = q[0] * inv;
-      o[3 + 3 * d] = m;
-      o[4 + 3 * d] = sqrtf(fmaxf(0.f, q[1] * inv - m * m));
-      o[5 + 3 * d] = q[2] * inv;
+      const double *q = acc + r * 3 * D + 3 * d;
+      const double m = q[0] * inv;
+      o[3 + 3 * d] = (float)m;
+      o[4 + 3 * d] = (float)sqrt(fmax(0.0, q[1] * inv - m * m));
+      o[5 + 3 * d] = (float)(q[2] * inv);
     }
     for (int k = 0; k < N; ++k) o[3 + 3 * D + k] = k == n ? 1.f : 0.f;
   }
@@ -341,38 +343,38 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
   (void)F;
   cudaStream_t s = t->stream;
   // per-mode row statistics (every mode: the co-indexed means need them all)
-  std::vector<float *> bufs;
-  auto alloc = [&](size_t n) -> float * {
+  std::vector<double *> bufs;
+  auto alloc = [&](size_t n) -> double * {
     void *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(float)) != cudaSuccess) return nullptr;
-    bufs.push_back(static_cast<float *>(p));
-    return static_cast<float *>(p);
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess) return nullptr;
+    bufs.push_back(static_cast<double *>(p));
+    return static_cast<double *>(p);
   };
   auto release = [&]() {
-    for (float *p : bufs) cudaFree(p);
+    for (double *p : bufs) cudaFree(p);
   };
-  std::vector<float *> cnt(N), s1(N), s2(N), lc(N);
+  std::vector<double *> cnt(N), s1(N), s2(N), mu(N), lc(N);
   for (int m = 0; m < N; ++m) {
     cnt[m] = alloc(t->rows[m]);
     s1[m] = alloc(t->rows[m]);
     s2[m] = alloc(t->rows[m]);
+    mu[m] = alloc(t->rows[m]);
     lc[m] = alloc(t->rows[m]);
-    if (!cnt[m] || !s1[m] || !s2[m] || !lc[m]) {
+    if (!cnt[m] || !s1[m] || !s2[m] || !mu[m] || !lc[m]) {
       release();
       return fail(GTK_ERR_OOM, "warm-start feature buffers");
     }
   }
-  float *raw_s1 = alloc(t->rows[n]);
-  float *acc = alloc(t->rows[n] * 3 * (size_t)std::max(1, D));
-  if (!raw_s1 || !acc) {
+  double *acc = alloc(t->rows[n] * 3 * (size_t)std::max(1, D));
+  if (!acc) {
     release();
     return fail(GTK_ERR_OOM, "warm-start feature buffers");
   }
   int rc = 0;
   for (int m = 0; m < N && !rc; ++m) {
-    rc = ck(cudaMemsetAsync(cnt[m], 0, t->rows[m] * 4, s), "memset");
-    if (!rc) rc = ck(cudaMemsetAsync(s1[m], 0, t->rows[m] * 4, s), "memset");
-    if (!rc) rc = ck(cudaMemsetAsync(s2[m], 0, t->rows[m] * 4, s), "memset");
+    rc = ck(cudaMemsetAsync(cnt[m], 0, t->rows[m] * 8, s), "memset");
+    if (!rc) rc = ck(cudaMemsetAsync(s1[m], 0, t->rows[m] * 8, s), "memset");
+    if (!rc) rc = ck(cudaMemsetAsync(s2[m], 0, t->rows[m] * 8, s), "memset");
     if (rc || !t->nnz) continue;
     const unsigned g = (unsigned)((t->nnz + (uint64_t)kChunk * kWsThreads - 1) / ((uint64_t)kChunk * kWsThreads));
     if (t->dtype == GTK_F32)
@@ -383,12 +385,11 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
                                                   s2[m]);
     rc = ck(cudaGetLastError(), "k_row_stats");
   }
-  if (!rc) rc = ck(cudaMemcpyAsync(raw_s1, s1[n], t->rows[n] * 4, cudaMemcpyDeviceToDevice, s), "copy");
   for (int m = 0; m < N && !rc; ++m) {
-    k_row_mean<<<grid_for(t->rows[m]), kWsThreads, 0, s>>>(cnt[m], s1[m], lc[m], t->rows[m]);
+    k_row_mean<<<grid_for(t->rows[m]), kWsThreads, 0, s>>>(cnt[m], s1[m], mu[m], lc[m], t->rows[m]);
     rc = ck(cudaGetLastError(), "k_row_mean");
   }
-  if (!rc) rc = ck(cudaMemsetAsync(acc, 0, t->rows[n] * 3 * (size_t)std::max(1, D) * 4, s), "memset");
+  if (!rc) rc = ck(cudaMemsetAsync(acc, 0, t->rows[n] * 3 * (size_t)std::max(1, D) * 8, s), "memset");
   if (!rc && t->nnz && D > 0) {
     CoArgs a;
     memset(&a, 0, sizeof(a));
@@ -398,7 +399,7 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
     for (int m = 0; m < N; ++m) {
       if (m == n) continue;
       a.coord[d] = t->vidx[n][m];
-      a.mu[d] = s1[m];
+      a.mu[d] = mu[m];
       a.lc[d] = lc[m];
       ++d;
     }
@@ -407,7 +408,7 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
     rc = ck(cudaGetLastError(), "k_coindex");
   }
   if (!rc) {
-    k_features<<<grid_for(t->rows[n]), kWsThreads, 0, s>>>(cnt[n], raw_s1, s2[n], acc, t->rows[n], N, n,
+    k_features<<<grid_for(t->rows[n]), kWsThreads, 0, s>>>(cnt[n], s1[n], s2[n], acc, t->rows[n], N, n,
                                                            3 + 3 * D + N, d_feat);
     rc = ck(cudaGetLastError(), "k_features");
   }
