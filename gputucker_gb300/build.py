@@ -28,7 +28,7 @@ CLI = os.path.join(BINDIR, "gputucker_gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
-LIB_SOURCES = ["api.cpp", "parse.cpp", "gen.cpp", "partition.cu", "sweep.cu", "tc_sweep.cu", "noalloc.cu", "batch.cu", "plan.cpp", "warmstart.cu"]
+LIB_SOURCES = ["api.cpp", "parse.cpp", "gen.cpp", "partition.cu", "sweep.cu", "tc_sweep.cu", "noalloc.cu", "batch.cu", "plan.cpp", "warmstart.cu", "tc_stream.cu"]
 
 
 def _nvcc() -> str:

@@ -90,6 +90,8 @@ static int put_core(DevTensor &t, const void *core) {
   GTK_CUDA(cudaMemcpyAsync(t.core, core, t.core_n * t.vsize, cudaMemcpyHostToDevice, t.stream));
   if (int rc = upload_core_perms(t, core)) return rc;
   t.have_core = true;
+  if (t.precision == GTK_PREC_BF16 && ts_supported(t.N, t.J, t.dtype, t.precision))
+    if (int rc = ts_build_images(t)) return rc;
   return 0;
 }
 
@@ -470,9 +472,12 @@ int gtk_set_precision(gtk_tensor *t, int precision) {
     return fail(GTK_ERR_ARG, "unknown precision");
   t->fit_from_store = false;
   drop_graph(*t);
-  if (precision != GTK_PREC_PLAIN && !tc_supported(t->N, t->J, t->dtype))
-    return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this order/rank/value type (FP32, N = 3 or 4, "
-                                     "J in {4, 8, 10, 12, 16} for N = 3 and {4, 8, 10, 12} for N = 4)");
+  if (precision != GTK_PREC_PLAIN && !tc_supported(t->N, t->J, t->dtype, precision))
+    return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this order/rank/value type/precision (FP32; "
+                                     "BF16 or TF32: N = 3, J in {4, 8, 10, 12, 16}; N = 4, J in {4, 8, 10, 12}; "
+                                     "BF16 only: N = 4, J = 16; N = 5, J in {4, 8, 12, 16})");
+  if (precision == GTK_PREC_BF16 && t->have_core && ts_supported(t->N, t->J, t->dtype, precision))
+    if (int rc = ts_build_images(*t)) return rc;
   t->precision = precision;
   if (precision == GTK_PREC_PLAIN && t->variant == kVarTc) t->variant = kVarAuto;
   return 0;

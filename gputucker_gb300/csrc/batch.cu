@@ -206,7 +206,7 @@ int gtk_autotune(gtk_tensor *t, int *variant) {
     }
     if (!cached && t->nnz) {
       std::vector<int> cands;
-      if (t->precision != GTK_PREC_PLAIN && tc_supported(t->N, t->J, t->dtype)) cands.push_back(kVarTc);
+      if (t->precision != GTK_PREC_PLAIN && tc_supported(t->N, t->J, t->dtype, t->precision)) cands.push_back(kVarTc);
       cands.push_back(kVarSpec2);
       cands.push_back(kVarSpec1);
       const size_t bytes = t->rows[0] * (size_t)t->ldf * t->vsize;

