@@ -27,7 +27,9 @@ LIB = os.path.join(LIBDIR, "libgputucker_gb300.so")
 CLI = os.path.join(BINDIR, "gputucker_gb300")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+# host code without FP contraction: the serial value_t sums that restate the
+# reference's (its norm) must round every product and sum separately
+COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
 LIB_SOURCES = ["api.cpp", "parse.cpp", "gen.cpp", "partition.cu", "sweep.cu", "tc_sweep.cu", "noalloc.cu", "batch.cu", "plan.cpp", "warmstart.cu", "tc_stream.cu"]
 
 

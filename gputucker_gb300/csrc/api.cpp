@@ -9,6 +9,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -320,7 +321,22 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
     if ((rc = ck(cudaMemsetAsync(t->corep[n], 0, (core_n / rank) * t->ldf * vs, t->stream), "memset"))) return bail(rc);
   }
   if ((rc = ck(cudaMemsetAsync(t->status, 0, 16, t->stream), "memset"))) return bail(rc);
-  if ((rc = build_partition(*t, *coo))) return bail(rc);
+  // the reference's norm (tensor_manager.tpp:263-293: NormX += val * val in value_t,
+  // input order, sqrt in value_t) on a host thread while the GPU partitions
+  std::thread norm_thread([t, coo]() {
+    if (coo->dtype == GTK_F32) {
+      float s = 0.f;
+      for (float v : coo->vf) s += v * v;
+      t->norm_ref = (double)std::sqrt(s);
+    } else {
+      double s = 0.0;
+      for (double v : coo->vd) s += v * v;
+      t->norm_ref = std::sqrt(s);
+    }
+  });
+  rc = build_partition(*t, *coo);
+  norm_thread.join();
+  if (rc) return bail(rc);
   *out = t;
   return 0;
   GTK_GUARD_END

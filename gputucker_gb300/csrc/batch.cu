@@ -168,7 +168,7 @@ extern "C" {
 
 int gtk_set_kernel_variant(gtk_tensor *t, int variant) {
   if (!t) return fail(GTK_ERR_ARG, "null tensor");
-  if (variant < GTK_VARIANT_AUTO || variant > GTK_VARIANT_TENSOR_CORE) return fail(GTK_ERR_ARG, "unknown variant");
+  if (variant < GTK_VARIANT_AUTO || variant > GTK_VARIANT_REFERENCE_ORDER) return fail(GTK_ERR_ARG, "unknown variant");
   if (variant == GTK_VARIANT_TENSOR_CORE && t->precision == GTK_PREC_PLAIN)
     return fail(GTK_ERR_UNSUPPORTED, "the tensor-core variant needs a precision form (gtk_set_precision)");
   t->variant = variant;
@@ -318,7 +318,7 @@ int gtk_batch_sweep(gtk_batch *b, double *fits) {
       gtk_tensor *t = b->ts[i];
       if (st[i] & 4) t->lu_fallbacks += 1;
       worst |= st[i];
-      if (fits) fits[i] = t->norm == 0 ? 1.0 : 1.0 - std::sqrt(std::max(0.0, err[i])) / t->norm;
+      if (fits) fits[i] = fit_from_err(*t, err[i]);
     }
     if (worst & 2) return fail(GTK_ERR_CUDA, "a tensor-core kernel gave up waiting for its MMAs");
     if (worst & 1) return fail(GTK_ERR_NUMERIC, "a row system was singular (zero LU pivot)");

@@ -19,8 +19,10 @@ constexpr int kVarSpec2 = 0;    // specialised SIMT kernel, 2 nonzeros per threa
 constexpr int kVarSpec1 = 1;    // specialised SIMT kernel, 1 nonzero per thread
 constexpr int kVarGeneric = 2;  // runtime-(N, J) SIMT kernel
 constexpr int kVarTc = 3;       // tcgen05 kernel (precision forms)
+constexpr int kVarRefOrder = 4;  // generic kernel, delta in the reference's operation order
 static_assert(kVarAuto == GTK_VARIANT_AUTO && kVarSpec2 == GTK_VARIANT_SIMT2 && kVarSpec1 == GTK_VARIANT_SIMT1 &&
-                  kVarGeneric == GTK_VARIANT_GENERIC && kVarTc == GTK_VARIANT_TENSOR_CORE,
+                  kVarGeneric == GTK_VARIANT_GENERIC && kVarTc == GTK_VARIANT_TENSOR_CORE &&
+                  kVarRefOrder == GTK_VARIANT_REFERENCE_ORDER,
               "variant codes of the C ABI");
 constexpr int kFitSumSlot = 1024;  // partial[] index of a fit's error sum
 // constants.hpp:18 declares kLambda as a double initialised from the float
@@ -113,6 +115,7 @@ struct DevTensor {
   uint64_t rows[kMaxOrder] = {};
   uint64_t core_n = 1;
   double norm = 0;
+  double norm_ref = 0;  // the reference's ||X||: value_t serial sum of x^2 in input order, sqrt in value_t
   int precision = GTK_PREC_PLAIN;
   bool have_factors = false, have_core = false;
 
@@ -169,7 +172,8 @@ int run_update_mode(DevTensor &t, int mode);
 int run_fit(DevTensor &t, double *fit);
 int run_delta(DevTensor &t, int mode, void *d_delta_blockmajor);
 int run_sweep(DevTensor &t, double *fit);
-int run_fit_enqueue(DevTensor &t);  // the fit kernels only; the sum lands in partial[kFitSumSlot]
+int run_fit_enqueue(DevTensor &t);
+double fit_from_err(const DevTensor &t, double err);  // fit = 1 - sqrt(err) / ||X|| (the variant's formula)  // the fit kernels only; the sum lands in partial[kFitSumSlot]
 int run_row_stats(DevTensor &t, int mode, uint32_t *max_count);
 int ensure_dstore(DevTensor &t);
 void drop_graph(DevTensor &t);

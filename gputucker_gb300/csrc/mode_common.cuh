@@ -36,6 +36,8 @@ struct ModeArgs {
   int others[kMaxOrder];             // the other modes in increasing order
   uint64_t gp_elems;                 // J^(N-1) * ldf
   int gp_in_smem;                    // generic kernel: core in shared memory?
+  int ref_order;                     // generic kernel: delta in the reference's operation order
+  const void *core;                  // the core, linear order (last mode fastest): ref_order
 };
 
 // ---------------------------------------------------------------- vector loads
@@ -115,6 +117,8 @@ __device__ void fill_pairs(unsigned char *pi, unsigned char *pj, int J) {
 // an un-contractible product (never fused into an FMA with the following add)
 __device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
 
 template <class V> struct ProdSum {
   double s = 0;
@@ -186,15 +190,22 @@ __device__ void gram_phase(const ModeArgs &a, const TileSmem<V> &s, uint64_t til
     const int sgi = w / E, e = w - sgi * E;
     const int i = s.pi[e], j = s.pj[e];
     const int t0 = (int)s.seg[sgi], t1 = (int)s.seg[sgi + 1];
-    ProdSum<V> acc;
-    for (int t = t0; t < t1; ++t) acc.add(mul_rn(s.dx[t * ldd + i], s.dx[t * ldd + j]));
+    double sum;
+    if (a.ref_order) {  // ComputingBC (update.cuh:85-90): value_t products added in double, in view order
+      sum = 0;
+      for (int t = t0; t < t1; ++t) sum += (double)mul_rn(s.dx[t * ldd + i], s.dx[t * ldd + j]);
+    } else {
+      ProdSum<V> acc;
+      for (int t = t0; t < t1; ++t) acc.add(mul_rn(s.dx[t * ldd + i], s.dx[t * ldd + j]));
+      sum = acc.value();
+    }
     const uint32_t row = s.rows[t0];
     double *dst = a.gram + (size_t)row * E + e;
     const bool shared_row = (sgi == 0 && first_open) || (sgi == nseg - 1 && last_open);
     if (shared_row)
-      atomicAdd(dst, acc.value());
+      atomicAdd(dst, sum);
     else
-      *dst = acc.value();
+      *dst = sum;
   }
 }
 

@@ -316,7 +316,42 @@ __global__ void __launch_bounds__(kThreads) k_mode_gen(ModeArgs a) {
       ap[k] = reinterpret_cast<const V *>(a.fac[o]) + (size_t)a.coord[o][gi] * ldf;
     }
     V xhat = V(0);
-    for (int jn = 0; jn < J; ++jn) {
+    if (a.ref_order) {
+      // computing_delta_kernel (delta.cuh:62-90): over the core entries i in linear
+      // order, beta = G_i * A_k[x_k][g_k(i)] for k = 0..N-1 skipping the mode, each
+      // product rounded, then tmp[g_mode(i)] += beta -- the same roundings in the
+      // same order, so FP32 delta is bit-identical to the reference's
+      V tmp[kMaxRank];
+      for (int j = 0; j < J; ++j) tmp[j] = V(0);
+      const V *G = reinterpret_cast<const V *>(a.core);
+      const V *fk[kMaxOrder];
+      for (int k = 0; k < a.N; ++k)
+        fk[k] = reinterpret_cast<const V *>(a.fac[k]) + (size_t)(valid ? a.coord[k][gi] : 0) * ldf;
+      int dig[kMaxOrder];
+      for (int k = 0; k < a.N; ++k) dig[k] = 0;
+      uint64_t ncore = 1;
+      for (int k = 0; k < a.N; ++k) ncore *= (uint64_t)J;
+      for (uint64_t i = 0; i < ncore; ++i) {
+        V beta = G[i];
+        for (int k = 0; k < a.N; ++k)
+          if (k != a.mode) beta = mul_rn(beta, fk[k][dig[k]]);
+        tmp[dig[a.mode]] = add_rn(tmp[dig[a.mode]], beta);
+        for (int k = a.N - 1; k >= 0; --k) {  // last mode fastest
+          if (++dig[k] < J) break;
+          dig[k] = 0;
+        }
+      }
+      for (int jn = 0; jn < J; ++jn) {
+        if (KIND == kUpdate) {
+          s.dx[tid * a.ldd + jn] = tmp[jn];
+        } else if (KIND == kFit) {
+          if (valid) xhat += tmp[jn] * facn[(size_t)row * ldf + jn];
+        } else {
+          if (valid) reinterpret_cast<V *>(a.out)[(size_t)a.vperm[gi] * J + jn] = tmp[jn];
+        }
+      }
+    }
+    for (int jn = 0; jn < J && !a.ref_order; ++jn) {
       V acc = V(0);
       if (M == 0) {
         acc = gp[jn];
@@ -627,6 +662,172 @@ __global__ void k_solve_lu_rows(const double *__restrict__ gram, const uint32_t 
   }
 }
 
+// ComputingBC (update.cuh:52-100) in the reference's order, for the
+// reference-order variant: one thread per (row, packed entry); B starts at lambda
+// on the diagonal, then every product delta_i * delta_j (C: delta_i * x), rounded
+// to value_t, is added in double over the row's nonzeros in view order -- block
+// order, then the block's where_nnz order, as the reference walks them.  delta
+// comes from the mode pass's store ([nnz][J], view order).
+template <class V>
+__global__ void k_bc_ref(const V *__restrict__ delta, const V *__restrict__ val, const uint32_t *__restrict__ row_of,
+                         uint64_t nnz, uint64_t rows, int J, int E, double lambda, double *__restrict__ gram) {
+  const uint64_t total = rows * (uint64_t)E;
+  for (uint64_t w = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; w < total;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t row = w / E;
+    const int e = (int)(w % E);
+    int i, j;
+    pair_of(e, J, i, j);
+    // [s, f): the row's nonzeros in the view (sorted by row)
+    uint64_t lo = 0, hi = nnz;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (row_of[mid] < row) lo = mid + 1; else hi = mid;
+    }
+    const uint64_t s0 = lo;
+    hi = nnz;
+    while (lo < hi) {
+      const uint64_t mid = (lo + hi) >> 1;
+      if (row_of[mid] <= row) lo = mid + 1; else hi = mid;
+    }
+    double sum = (i == j) ? lambda : 0.0;
+    for (uint64_t t = s0; t < lo; ++t) {
+      const V di = delta[t * J + i];
+      const V dj = j == J ? val[t] : delta[t * J + j];
+      sum = __dadd_rn(sum, (double)mul_rn(di, dj));
+    }
+    gram[row * E + e] = sum;
+  }
+}
+
+// The reference's row solve (update.cuh:163-194) in its own operation order, for
+// the reference-order variant: B^-1 from LU with row pivoting (first largest
+// pivot) and a solve of the permuted identity, then a_k = sum_l C_l B^-1(l, k)
+// accumulated in value_t (`value_t res += C * B_inv`): every product and sum
+// rounded separately, no fused multiply-adds.  One warp per row; lane c owns
+// column c of the inverse.
+template <class V>
+__global__ void k_solve_ref_rows(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf,
+                                 V *__restrict__ fac, double lambda) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  double *A = sm + (size_t)wib * (2 * (size_t)J * J + 2 * J);
+  double *b = A + (size_t)J * J;
+  double *inv = b + J;            // [J][J], inv[i * J + c]
+  double *perm = inv + (size_t)J * J;  // row permutation, as doubles
+  for (uint64_t row = (uint64_t)blockIdx.x * wpb + wib; row < rows; row += (uint64_t)gridDim.x * wpb) {
+    load_system(gram + row * E, J, E, lambda, A, b, lane);
+    for (int i = lane; i < J; i += 32) perm[i] = (double)i;
+    __syncwarp();
+    for (int k = 0; k < J; ++k) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + lane; i < J; i += 32) {
+        const double v = fabs(A[i * J + k]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xFFFFFFFFu, best, o);
+        const int oi = __shfl_xor_sync(0xFFFFFFFFu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (bi != k) {
+        for (int c = lane; c < J; c += 32) {
+          const double tmp = A[k * J + c];
+          A[k * J + c] = A[bi * J + c];
+          A[bi * J + c] = tmp;
+        }
+        if (lane == 0) {
+          const double tp = perm[k];
+          perm[k] = perm[bi];
+          perm[bi] = tp;
+        }
+      }
+      __syncwarp();
+      const double d = A[k * J + k];
+      if (d != 0.0) {
+        for (int i = k + 1 + lane; i < J; i += 32) {
+          const double f = __ddiv_rn(A[i * J + k], d);
+          A[i * J + k] = f;
+          for (int c = k + 1; c < J; ++c) A[i * J + c] = __dsub_rn(A[i * J + c], __dmul_rn(f, A[k * J + c]));
+        }
+      }
+      __syncwarp();
+    }
+    for (int col = lane; col < J; col += 32) {
+      for (int i = 0; i < J; ++i) {
+        double sacc = ((int)perm[i] == col) ? 1.0 : 0.0;
+        for (int c = 0; c < i; ++c) sacc = __dsub_rn(sacc, __dmul_rn(A[i * J + c], inv[c * J + col]));
+        inv[i * J + col] = sacc;
+      }
+      for (int i = J - 1; i >= 0; --i) {
+        double sacc = inv[i * J + col];
+        for (int c = i + 1; c < J; ++c) sacc = __dsub_rn(sacc, __dmul_rn(A[i * J + c], inv[c * J + col]));
+        inv[i * J + col] = __ddiv_rn(sacc, A[i * J + i]);
+      }
+    }
+    __syncwarp();
+    V *frow = fac + row * ldf;
+    for (int k = lane; k < ldf; k += 32) {
+      V res = V(0);
+      if (k < J)
+        for (int l = 0; l < J; ++l) res = (V)__dadd_rn((double)res, __dmul_rn(b[l], inv[l * J + k]));
+      frow[k] = res;
+    }
+    __syncwarp();
+  }
+}
+
+// Reconstruction in the reference's order, for the reference-order variant
+// (ComputingReconstructionKernel, reconstruction.cuh:58-81): per nonzero of the
+// last mode's view, x_hat = sum over core entries i in linear order of
+// G_i * A_0[x_0][g_0(i)] * ... * A_{N-1}[x_{N-1}][g_{N-1}(i)], every product and sum
+// rounded; written to the nonzero's block-major position.
+template <class V>
+__global__ void k_recon_ref(ModeArgs a, V *__restrict__ xhat) {
+  const int J = a.J, N = a.N, ldf = a.ldf;
+  const V *G = reinterpret_cast<const V *>(a.core);
+  uint64_t ncore = 1;
+  for (int k = 0; k < N; ++k) ncore *= (uint64_t)J;
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < a.nnz; t += (uint64_t)gridDim.x * blockDim.x) {
+    const V *fk[kMaxOrder];
+    for (int k = 0; k < N; ++k) fk[k] = reinterpret_cast<const V *>(a.fac[k]) + (size_t)a.coord[k][t] * ldf;
+    int dig[kMaxOrder];
+    for (int k = 0; k < N; ++k) dig[k] = 0;
+    V res = V(0);
+    for (uint64_t i = 0; i < ncore; ++i) {
+      V temp = G[i];
+      for (int k = 0; k < N; ++k) temp = mul_rn(temp, fk[k][dig[k]]);
+      res = add_rn(res, temp);
+      for (int k = N - 1; k >= 0; --k) {
+        if (++dig[k] < J) break;
+        dig[k] = 0;
+      }
+    }
+    xhat[a.vperm[t]] = res;
+  }
+}
+
+// the reference's error loop (reconstruction.cuh:259-268): one thread, block-major
+// order, Error += (x - x_hat)^2 in value_t -- serial like the reference's
+template <class V>
+__global__ void k_err_ref(const V *__restrict__ val, const V *__restrict__ xhat, uint64_t nnz, double *__restrict__ out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  V err = V(0);
+  for (uint64_t t = 0; t < nnz; ++t) {
+    const V e = val[t] - xhat[t];
+    err = add_rn(err, mul_rn(e, e));
+  }
+  *out = (double)err;
+}
+
 // the fit from the delta of the last mode's pass (stored in view order):
 // x_hat = delta . a_{N-1}[i_{N-1}] in value_t (reconstruction.cuh:58-81 reduced to
 // one dot product), error (x - x_hat)^2 summed in FP64 per CTA
@@ -708,10 +909,19 @@ constexpr int kThreadSolveMaxJ = 24;  // larger ranks solve one row per warp
 // this are solved in FP64 (one FP32 refinement step leaves ~(kappa * 2^-24)^2)
 constexpr float kCondMaxFp32 = 1e5f;
 
-// kernel of a KIND: the update honours the handle's variant (set by the autotuner)
+// kernel of a KIND: the update honours the handle's variant (set by the autotuner);
+// the reference-order variant applies to every KIND
 template <class V, int KIND> int choose(Launch &L, const DevTensor &t, bool &gp_in_smem) {
   gp_in_smem = true;
-  const int var = KIND == kUpdate ? t.variant : kVarAuto;
+  const int var = (KIND == kUpdate || t.variant == kVarRefOrder) ? t.variant : kVarAuto;
+  if (var == kVarRefOrder) {
+    L.spec = false;
+    L.tn = kThreads;
+    L.fn = (const void *)k_mode_gen<V, KIND>;
+    gp_in_smem = false;
+    L.smem = tile_smem_bytes(sizeof(V), 0, 0, 1, t.J, ldd_for(t.J), pairs_for(t.J), kThreads);
+    return 0;
+  }
   if (var == kVarSpec1) {
     if (find_spec<V, KIND, 1>(L, t) && L.smem <= kSmemLimit) return 0;
   } else if (var != kVarGeneric) {
@@ -815,6 +1025,8 @@ template <class V, int KIND> static int launch_mode(DevTensor &t, int mode, void
   if (int rc = prepare_fn(L.fn, L.smem)) return rc;
   ModeArgs a = make_args(t, mode);
   a.gp_in_smem = gp_in_smem ? 1 : 0;
+  a.ref_order = t.variant == kVarRefOrder ? 1 : 0;
+  a.core = t.core;
   if (KIND == kUpdate)
     a.dstore = out;  // optional: delta of every nonzero, view order
   else
@@ -850,8 +1062,9 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   const int J = t.J;
   const bool last = mode == t.N - 1;
   // the last mode's pass also stores delta, from which the sweep's fit follows exactly
+  // (the reference-order variant stores it on every mode: its B and C come from it)
   void *dstore = nullptr;
-  if (last && t.nnz) {
+  if ((last || t.variant == kVarRefOrder) && t.nnz) {
     if (int rc = ensure_dstore(t)) return rc;
     dstore = t.dstore;
   }
@@ -875,7 +1088,30 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   const int lu_wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (48 * 1024) / lu_warp));
   const size_t lu_smem = lu_warp * lu_wpb;
   if (int rc = prepare_fn((const void *)k_solve_lu_rows<V>, lu_smem)) return rc;
-  if (J <= kThreadSolveMaxJ) {
+  if (t.variant == kVarRefOrder) {
+    // B and C again, in the reference's summation order, from the stored delta
+    if (!t.dstore) return fail(GTK_ERR_OOM, "the reference-order variant needs room for delta ([nnz][J])");
+    if (t.nnz) {
+      const uint64_t total = t.rows[mode] * (uint64_t)E;
+      const unsigned g = (unsigned)std::min<uint64_t>((total + 255) / 256, (uint64_t)t.num_sms * 64);
+      k_bc_ref<V><<<g, 256, 0, t.stream>>>((const V *)t.dstore, (const V *)t.vval[mode], t.vidx[mode][mode], t.nnz,
+                                           t.rows[mode], J, E, kLambda, t.gram);
+      GTK_CUDA(cudaGetLastError());
+      t.launches += 1;
+    }
+    // the reference's inverse-then-multiply with value_t accumulation (update.cuh:163-194);
+    // lambda is already on the diagonal
+    const size_t per_warp = (2 * (size_t)J * J + 2 * J) * 8;
+    const int wpb = (int)std::min<size_t>(8, std::max<size_t>(1, (96 * 1024) / per_warp));
+    const size_t smem = per_warp * wpb;
+    if (int rc = prepare_fn((const void *)k_solve_ref_rows<V>, smem)) return rc;
+    uint64_t grid = std::min<uint64_t>((t.rows[mode] + wpb - 1) / wpb, (uint64_t)t.num_sms * 32);
+    if (grid < 1) grid = 1;
+    k_solve_ref_rows<V><<<(unsigned)grid, wpb * 32, smem, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf,
+                                                                      (V *)t.fac[mode], t.nnz ? 0.0 : kLambda);
+    GTK_CUDA(cudaGetLastError());
+    t.launches += 1;
+  } else if (J <= kThreadSolveMaxJ) {
     const int T = J <= 12 ? 128 : 64;
     const size_t smem = (size_t)T * E * 8;
     if (int rc = prepare_fn((const void *)k_solve_rows<V>, smem)) return rc;
@@ -911,7 +1147,7 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
     GTK_CUDA(cudaGetLastError());
     t.launches += 1;
   }
-  t.fit_from_store = dstore != nullptr;
+  t.fit_from_store = dstore != nullptr && last;
   if (int rc = prof_end(t, 1, ev)) return rc;
   return 0;
 }
@@ -923,6 +1159,20 @@ int run_update_mode(DevTensor &t, int mode) {
 // the fit kernels: the error of every nonzero summed into t.partial[kFitGridMax]
 template <class V> static int fit_enqueue(DevTensor &t) {
   int grid = 1;
+  if (t.variant == kVarRefOrder && t.nnz) {
+    // x_hat into the delta store's memory (nnz values), then the serial error
+    if (int rc = ensure_dstore(t)) return rc;
+    if (!t.dstore) return fail(GTK_ERR_OOM, "the reference-order fit needs nnz values of scratch");
+    ModeArgs a = make_args(t, t.N - 1);
+    a.core = t.core;
+    const unsigned g = (unsigned)std::min<uint64_t>((t.nnz + 255) / 256, (uint64_t)t.num_sms * 16);
+    k_recon_ref<V><<<g, 256, 0, t.stream>>>(a, (V *)t.dstore);
+    k_err_ref<V><<<1, 32, 0, t.stream>>>((const V *)t.blk_val, (const V *)t.dstore, t.nnz, t.partial + kFitGridMax);
+    GTK_CUDA(cudaGetLastError());
+    t.launches += 2;
+    t.fit_from_store = false;  // the store now holds x_hat
+    return 0;
+  }
   if (t.fit_from_store && t.nnz) {
     grid = (int)std::min<uint64_t>(kFitGridMax, (t.nnz + 255) / 256);
     k_fit_stored<V><<<grid, 256, 0, t.stream>>>((const V *)t.dstore, t.vidx[t.N - 1][t.N - 1], (const V *)t.vval[t.N - 1],
@@ -945,11 +1195,24 @@ template <class V> static int fit_enqueue(DevTensor &t) {
   return 0;
 }
 
+double fit_from_err(const DevTensor &t, double err) {
+  if (t.variant == kVarRefOrder && t.nnz) {
+    // reconstruction.cuh:272-276 with the reference's value_t Error and norm
+    if (t.norm_ref == 0) return 1.0;
+    if (t.dtype == GTK_F32) {
+      const float e = (float)err, nr = (float)t.norm_ref;
+      return (double)(1.0f - std::sqrt(e) / nr);
+    }
+    return 1.0 - std::sqrt(err) / t.norm_ref;
+  }
+  return (t.norm == 0) ? 1.0 : 1.0 - std::sqrt(std::max(0.0, err)) / t.norm;
+}
+
 static int fit_read(DevTensor &t, double *fit) {
   double err = 0;
   GTK_CUDA(cudaMemcpyAsync(&err, t.partial + kFitGridMax, 8, cudaMemcpyDeviceToHost, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
-  *fit = (t.norm == 0) ? 1.0 : 1.0 - std::sqrt(err) / t.norm;
+  *fit = fit_from_err(t, err);
   return 0;
 }
 

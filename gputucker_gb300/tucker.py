@@ -270,10 +270,10 @@ class BlockedTensor:
         k = min(n.value, fits_cap)
         return [f[i] for i in range(k)]
 
-    VARIANTS = {"auto": -1, "simt2": 0, "simt1": 1, "generic": 2, "tensor_core": 3}
+    VARIANTS = {"auto": -1, "simt2": 0, "simt1": 1, "generic": 2, "tensor_core": 3, "reference_order": 4}
 
     def set_kernel_variant(self, variant: str) -> None:
-        """Force the update kernel ('auto', 'simt2', 'simt1', 'generic', 'tensor_core')."""
+        """Force the update kernel ('auto', 'simt2', 'simt1', 'generic', 'tensor_core', 'reference_order')."""
         call("gtk_set_kernel_variant", self.handle, self.VARIANTS[variant])
 
     def kernel_variant(self) -> str:

@@ -205,8 +205,11 @@ int gtk_checkpoint_info(const char *path, int *order, int *rank, int *dtype, uin
  * GTK_VARIANT_SIMT2 / SIMT1 (specialised SIMT kernels, 2 or 1 nonzeros per
  * thread; shapes without a specialisation run GENERIC), GTK_VARIANT_GENERIC
  * (runtime order and rank), GTK_VARIANT_TENSOR_CORE (tcgen05; needs a precision
- * form).  GTK_VARIANT_AUTO: tensor cores for the precision forms, SIMT2
- * otherwise.  gtk_set_kernel_variant forces one; gtk_autotune times the variants
+ * form), GTK_VARIANT_REFERENCE_ORDER (delta of the update, the fit and
+ * gtk_compute_delta in the reference's operation order, computing_delta_kernel,
+ * delta.cuh:62-90: core entries in linear order, products left to right, each
+ * rounded -- FP32 delta bit-identical to the reference's; slow, for parity).
+ * GTK_VARIANT_AUTO: tensor cores for the precision forms, SIMT2 otherwise.  gtk_set_kernel_variant forces one; gtk_autotune times the variants
  * that apply on the handle's mode-0 update (factor 0 restored afterwards), keeps
  * the fastest and caches it per (order, rank, value type, precision, log2 mean
  * row length, log2 longest/mean row length) for the process, so later handles
@@ -216,6 +219,7 @@ int gtk_checkpoint_info(const char *path, int *order, int *rank, int *dtype, uin
 #define GTK_VARIANT_SIMT1 1
 #define GTK_VARIANT_GENERIC 2
 #define GTK_VARIANT_TENSOR_CORE 3
+#define GTK_VARIANT_REFERENCE_ORDER 4
 int gtk_set_kernel_variant(gtk_tensor *t, int variant);
 int gtk_get_kernel_variant(const gtk_tensor *t, int *variant);
 int gtk_autotune(gtk_tensor *t, int *variant);
