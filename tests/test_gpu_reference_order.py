@@ -62,3 +62,28 @@ def test_reference_order_matches_reference(path):
             else:
                 assert abs(fit - float(g[f"fit{s + 1}"])) <= 1e-12
         assert np.array_equal(t.get_core(), g["core"])
+
+
+from test_gpu_parity import CASES, ILL, data  # noqa: E402
+
+
+@pytest.mark.parametrize("case", CASES + ILL, ids=[c[0] for c in CASES + ILL])
+def test_reference_order_bit_exact_vs_oracle(case):
+    """The oracle restates the reference's path bit for bit in FP32 (pinned against
+    the fixtures in test_oracle.py); the reference-order variant matches it bit for
+    bit too -- on every shape, including the Zipf-skewed cases where FP32 ALS is
+    chaotic and any other order of operations drifts by O(1)."""
+    from oracle_util import Oracle
+    name, dims, nnz, P, J, _ = case
+    idx, vals = data(case, 0)
+    with gtk.create_tensor_blocks(gtk.coo_from_arrays(idx, vals, dims=dims), P, J) as t:
+        ora = Oracle(0, idx, vals, dims, P, J)
+        t.init_random(1, 0)
+        ora.init_random(1, 0)
+        t.set_kernel_variant("reference_order")
+        for s in range(3):
+            fit = t.sweep()
+            of = ora.sweep()["fit_ref"]
+            for n in range(len(dims)):
+                assert np.array_equal(t.get_factor(n), ora.get_factor(n)), (name, s, n)
+            assert fit == of, (name, s, fit, of)
