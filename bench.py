@@ -65,6 +65,8 @@ def args_parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--nnz", type=int, default=None, help="override nnz (smaller runs)")
+    p.add_argument("--shape", type=str, default=None,
+                   help="ORDER,RANK,DIM[,P]: another Zipf tensor shape in place of the headline one (profiling)")
     p.add_argument("--e2e-runs", type=int, default=1)
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-cpu", action="store_true")
@@ -523,6 +525,12 @@ def run_warmstart(args, dist):
 def main():
     args = args_parse()
     cfg = dict(WORKLOAD)
+    if args.shape:
+        f = [int(x) for x in args.shape.split(",")]
+        order, rank, dim = f[0], f[1], f[2]
+        part = f[3] if len(f) > 3 else 1
+        cfg.update(workload=f"zipf{order}d_{dim}_rank{rank}_P{part}", order=order, dims=[dim] * order, rank=rank,
+                   partition=[part] * order)
     dist = Dist(args.impl)
     if args.impl == "reference":
         run_reference(args, cfg, dist)
@@ -572,7 +580,7 @@ def main():
         with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
             tr = json.load(f)
         key = "plain" if chosen == "plain" else "tc"
-        if key in tr:
+        if key in tr and not args.shape:
             traffic = tr[key]["mean_bytes_per_launch"] * nnz / tr["nnz"]
     except Exception:
         pass
@@ -581,7 +589,8 @@ def main():
         compute = {"fp32_simt_tflops": flops / per_launch_s / 1e12, "fp32_simt_peak_tflops_nominal": 80.6}
     else:
         kp = (J * J + 15) // 16 * 16
-        flops = nnz * 2 * kp * kp  # the tcgen05 GEMM as issued (K = N = J^2 padded to 16)
+        cols = (J ** (N - 2) + 15) // 16 * 16
+        flops = nnz * 2 * kp * cols  # the tcgen05 GEMM as issued (K = J^2, J^(N-2) columns, padded to 16)
         tpeak = peaks.get("bf16_tflops", 1914.6) * (1.0 if chosen == "bf16" else 0.5)
         compute = {"tensor_tflops": flops / per_launch_s / 1e12, "tensor_peak_tflops": tpeak,
                    "tensor_frac": flops / per_launch_s / 1e12 / tpeak,
@@ -589,8 +598,8 @@ def main():
     roofline = {
         "bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s", "frac": achieved / hbm_peak,
         "traffic": traffic,
-        "kernel": ("k_mode_spec<float,4,10,2,kUpdate>" if chosen == "plain"
-                   else f"k_mode_tc<10,3,{chosen},update>") + " (fused delta + Gram/RHS)",
+        "kernel": (f"k_mode_spec<float,{N},{J},2,kUpdate>" if chosen == "plain"
+                   else f"k_mode_tc<{J},{N - 1},{chosen},update>") + " (fused delta + Gram/RHS)",
         "bytes_per_launch": bytes_per_launch, "bytes_note": "unfused delta: B_delta = 4N + 4J bytes per nonzero and mode",
         "launch_ms": per_launch_s * 1e3, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback",
     } | compute
