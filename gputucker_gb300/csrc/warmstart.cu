@@ -3,11 +3,13 @@
 // counterpart (the reference always starts from uniform [0,1) draws,
 // tucker.cuh:84-97; that stays the fallback).
 //
-// Features of row i of mode n (F = 3 + 3(N-1) + N values):
+// Features of row i of mode n (F = 4 + 6(N-1) + N values):
 //   log(1 + c_i), mean x, std x over the row's c_i nonzeros;
-//   for every other mode m (increasing): mean and std over the row's nonzeros of
-//   mu_m[i_m] (the mean value of the co-indexed row of mode m), and the mean of
-//   log(1 + c_m[i_m]) (its density);
+//   for every other mode m (increasing): over the row's nonzeros, the mean and std
+//   of mu_m[i_m] (the mean value of the co-indexed row of mode m), the mean of
+//   lc_m = log(1 + c_m[i_m]) (its density), and the cross moments E[x mu_m],
+//   E[x mu_m^2], E[x lc_m] (how the row's values vary with the co-indexed rows);
+//   E[x prod_m mu_m];
 //   one-hot of n.
 // Each feature is standardised with the mean/std of the training examples.
 //
@@ -117,41 +119,54 @@ __global__ void k_row_mean(const double *__restrict__ cnt, const double *__restr
   }
 }
 
+inline int ws_nfeat(int N) { return 4 + 6 * (N - 1) + N; }
+
 struct CoArgs {
   const uint32_t *row;             // view of mode n: global row of mode n
+  const void *val;                 // view of mode n: values
   const uint32_t *coord[kMaxOrder];  // view of mode n: coordinates of the other modes (compact, D entries)
   const double *mu[kMaxOrder];
   const double *lc[kMaxOrder];
   int D;
 };
 
-// per row of mode n, for each other mode: sum mu, sum mu^2, sum lc over the row's nonzeros
-__global__ void k_coindex(CoArgs a, uint64_t nnz, double *__restrict__ acc /* rows x 3D */) {
+// per row of mode n, for each other mode d: sums of mu, mu^2, lc, x mu, x mu^2,
+// x lc over the row's nonzeros (6 per mode), then the sum of x prod_d mu_d
+template <class V>
+__global__ void k_coindex(CoArgs a, uint64_t nnz, double *__restrict__ acc /* rows x (6D + 1) */) {
   const uint64_t t0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kChunk;
   if (t0 >= nnz) return;
   const uint64_t t1 = min(nnz, t0 + kChunk);
-  const int D = a.D;
+  const int D = a.D, W = 6 * D + 1;
+  const V *val = reinterpret_cast<const V *>(a.val);
   uint32_t r = a.row[t0];
-  double s[3 * (kMaxOrder - 1)];
-  for (int k = 0; k < 3 * D; ++k) s[k] = 0;
+  double s[6 * (kMaxOrder - 1) + 1];
+  for (int k = 0; k < W; ++k) s[k] = 0;
   for (uint64_t t = t0; t < t1; ++t) {
     const uint32_t rr = a.row[t];
     if (rr != r) {
-      for (int k = 0; k < 3 * D; ++k) {
-        atomicAdd(acc + (size_t)r * 3 * D + k, s[k]);
+      for (int k = 0; k < W; ++k) {
+        atomicAdd(acc + (size_t)r * W + k, s[k]);
         s[k] = 0;
       }
       r = rr;
     }
+    const double x = (double)val[t];
+    double prod = x;
     for (int d = 0; d < D; ++d) {
       const uint32_t c = a.coord[d][t];
-      const double m = a.mu[d][c];
-      s[3 * d] += m;
-      s[3 * d + 1] += m * m;
-      s[3 * d + 2] += a.lc[d][c];
+      const double m = a.mu[d][c], l = a.lc[d][c];
+      s[6 * d] += m;
+      s[6 * d + 1] += m * m;
+      s[6 * d + 2] += l;
+      s[6 * d + 3] += x * m;
+      s[6 * d + 4] += x * m * m;
+      s[6 * d + 5] += x * l;
+      prod *= m;
     }
+    s[6 * D] += prod;
   }
-  for (int k = 0; k < 3 * D; ++k) atomicAdd(acc + (size_t)r * 3 * D + k, s[k]);
+  for (int k = 0; k < W; ++k) atomicAdd(acc + (size_t)r * W + k, s[k]);
 }
 
 // raw features of rows [0, rows) of mode n, F per row
@@ -168,14 +183,19 @@ __global__ void k_features(const double *__restrict__ cnt, const double *__restr
     o[0] = (float)log1p(c);
     o[1] = (float)mean;
     o[2] = (float)sqrt(var);
+    const double *q0 = acc + r * (6 * D + 1);
     for (int d = 0; d < D; ++d) {
-      const double *q = acc + r * 3 * D + 3 * d;
+      const double *q = q0 + 6 * d;
       const double m = q[0] * inv;
-      o[3 + 3 * d] = (float)m;
-      o[4 + 3 * d] = (float)sqrt(fmax(0.0, q[1] * inv - m * m));
-      o[5 + 3 * d] = (float)(q[2] * inv);
+      o[3 + 6 * d] = (float)m;
+      o[4 + 6 * d] = (float)sqrt(fmax(0.0, q[1] * inv - m * m));
+      o[5 + 6 * d] = (float)(q[2] * inv);
+      o[6 + 6 * d] = (float)(q[3] * inv);
+      o[7 + 6 * d] = (float)(q[4] * inv);
+      o[8 + 6 * d] = (float)(q[5] * inv);
     }
-    for (int k = 0; k < N; ++k) o[3 + 3 * D + k] = k == n ? 1.f : 0.f;
+    o[3 + 6 * D] = (float)(q0[6 * D] * inv);
+    for (int k = 0; k < N; ++k) o[4 + 6 * D + k] = k == n ? 1.f : 0.f;
   }
 }
 
@@ -339,7 +359,7 @@ unsigned grid_for(uint64_t n, int threads = kWsThreads) {
 
 // raw features of every row of mode n into d_feat (rows[n] x F)
 int mode_features(gtk_tensor *t, int n, float *d_feat) {
-  const int N = t->N, D = N - 1, F = 3 + 3 * D + N;
+  const int N = t->N, D = N - 1, F = ws_nfeat(N);
   (void)F;
   cudaStream_t s = t->stream;
   // per-mode row statistics (every mode: the co-indexed means need them all)
@@ -365,7 +385,7 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
       return fail(GTK_ERR_OOM, "warm-start feature buffers");
     }
   }
-  double *acc = alloc(t->rows[n] * 3 * (size_t)std::max(1, D));
+  double *acc = alloc(t->rows[n] * (size_t)(6 * std::max(1, D) + 1));
   if (!acc) {
     release();
     return fail(GTK_ERR_OOM, "warm-start feature buffers");
@@ -389,11 +409,12 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
     k_row_mean<<<grid_for(t->rows[m]), kWsThreads, 0, s>>>(cnt[m], s1[m], mu[m], lc[m], t->rows[m]);
     rc = ck(cudaGetLastError(), "k_row_mean");
   }
-  if (!rc) rc = ck(cudaMemsetAsync(acc, 0, t->rows[n] * 3 * (size_t)std::max(1, D) * 8, s), "memset");
+  if (!rc) rc = ck(cudaMemsetAsync(acc, 0, t->rows[n] * (size_t)(6 * std::max(1, D) + 1) * 8, s), "memset");
   if (!rc && t->nnz && D > 0) {
     CoArgs a;
     memset(&a, 0, sizeof(a));
     a.row = t->vidx[n][n];
+    a.val = t->vval[n];
     a.D = D;
     int d = 0;
     for (int m = 0; m < N; ++m) {
@@ -404,12 +425,15 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
       ++d;
     }
     const unsigned g = (unsigned)((t->nnz + (uint64_t)kChunk * kWsThreads - 1) / ((uint64_t)kChunk * kWsThreads));
-    k_coindex<<<g, kWsThreads, 0, s>>>(a, t->nnz, acc);
+    if (t->dtype == GTK_F32)
+      k_coindex<float><<<g, kWsThreads, 0, s>>>(a, t->nnz, acc);
+    else
+      k_coindex<double><<<g, kWsThreads, 0, s>>>(a, t->nnz, acc);
     rc = ck(cudaGetLastError(), "k_coindex");
   }
   if (!rc) {
     k_features<<<grid_for(t->rows[n]), kWsThreads, 0, s>>>(cnt[n], s1[n], s2[n], acc, t->rows[n], N, n,
-                                                           3 + 3 * D + N, d_feat);
+                                                           F, d_feat);
     rc = ck(cudaGetLastError(), "k_features");
   }
   if (!rc) rc = ck(cudaStreamSynchronize(s), "sync");
@@ -477,7 +501,7 @@ int gtk_ws_create(int order, int rank, int hidden, uint64_t seed, int device, gt
   m->N = order;
   m->J = rank;
   m->H = hidden;
-  m->F = 3 + 3 * (order - 1) + order;
+  m->F = ws_nfeat(order);
   m->np = ws_np(m->F, m->H, m->J);
   m->seed = seed;
   auto bail = [&](int rc) {
@@ -571,7 +595,7 @@ int gtk_ws_features(gtk_tensor *t, int mode, float *out) {
   if (!t || !out || mode < 0 || mode >= t->N) return fail(GTK_ERR_ARG, "bad argument");
   if (t->N < 2) return fail(GTK_ERR_UNSUPPORTED, "warm start needs order >= 2");
   GTK_CUDA(cudaSetDevice(t->dev));
-  const int F = 3 + 3 * (t->N - 1) + t->N;
+  const int F = ws_nfeat(t->N);
   float *d = nullptr;
   GTK_CUDA(cudaMalloc(&d, std::max<size_t>(1, t->rows[mode] * F) * 4));
   int rc = mode_features(t, mode, d);

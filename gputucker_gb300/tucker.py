@@ -493,7 +493,7 @@ class WarmStart:
 
 def ws_features(t: BlockedTensor, mode: int) -> np.ndarray:
     """Raw warm-start features of every row of `mode` (rows x F)."""
-    F = 3 + 3 * (t.order - 1) + t.order
+    F = 4 + 6 * (t.order - 1) + t.order
     out = np.empty((t.factor_rows(mode), F), np.float32)
     call("gtk_ws_features", t.handle, mode, _ptr(out))
     return out

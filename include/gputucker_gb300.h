@@ -241,11 +241,12 @@ void gtk_batch_destroy(gtk_batch *b);
  * No reference counterpart (the reference starts from uniform [0,1) draws,
  * tucker.cuh:84-97, which stay the fallback).  A small MLP (two hidden ReLU
  * layers of `hidden` units) maps per-row statistics of a tensor to initial
- * factor rows.  Features of row i of mode n (F = 3 + 3(order-1) + order floats):
- * log(1+c_i), mean and std of the row's values; for each other mode m, mean and
- * std over the row's nonzeros of the co-indexed row's mean value, and mean of
- * log(1 + its nonzero count); one-hot of n.  Training and inference run in the
- * library's CUDA kernels (FP32, Adam).
+ * factor rows.  Features of row i of mode n (F = 4 + 6(order-1) + order floats):
+ * log(1+c_i), mean and std of the row's values; for each other mode m, over the
+ * row's nonzeros: mean and std of the co-indexed row's mean value mu_m, mean of
+ * lc_m = log(1 + its nonzero count), and the cross moments E[x mu_m],
+ * E[x mu_m^2], E[x lc_m]; E[x prod_m mu_m]; one-hot of n.  Training and
+ * inference run in the library's CUDA kernels (FP32, Adam).
  *   gtk_ws_add_example: the handle's current factors (converged by the plain
  *     method) become training targets for the features of its non-empty rows;
  *   gtk_ws_train: `steps` Adam steps on random batches of the examples (the

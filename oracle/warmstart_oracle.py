@@ -7,8 +7,9 @@ warm start has no reference counterpart (GPUTucker always starts from uniform
 in float64 numpy:
 
   features of row i of mode n: log(1+c_i), mean and std of its values; for each
-  other mode m (increasing): mean and std over the row's nonzeros of mu_m[i_m]
-  (the mean value of the co-indexed row of mode m) and mean of log(1+c_m[i_m]);
+  other mode m (increasing), over the row's nonzeros: mean and std of mu_m[i_m]
+  (the mean value of the co-indexed row of mode m), mean of lc_m = log(1+c_m[i_m]),
+  and the cross moments E[x mu_m], E[x mu_m^2], E[x lc_m]; E[x prod_m mu_m];
   one-hot of n.
   network: y = W3 relu(W2 relu(W1 x + b1) + b2) + b3; loss = mean (y - t)^2.
 """
@@ -19,41 +20,48 @@ import numpy as np
 
 
 def row_features(idx, vals, rows, mode):
-    """Raw features of every row [0, rows[mode]) of `mode` (float64), F = 3 + 3(N-1) + N."""
+    """Raw features of every row [0, rows[mode]) of `mode` (float64), F = 4 + 6(N-1) + N."""
     N = len(idx)
     vals = np.asarray(vals, np.float64)
-    cnt, mu, lc = [], [], []
+    mu, lc = [], []
     for m in range(N):
         c = np.bincount(idx[m], minlength=rows[m]).astype(np.float64)
         s = np.bincount(idx[m], weights=vals, minlength=rows[m])
-        cnt.append(c)
         mu.append(np.divide(s, c, out=np.zeros_like(s), where=c > 0))
         lc.append(np.log1p(c))
     n = mode
     R = rows[n]
-    c = cnt[n]
+    c = np.bincount(idx[n], minlength=R).astype(np.float64)
     inv = np.divide(1.0, c, out=np.zeros_like(c), where=c > 0)
-    s1 = np.bincount(idx[n], weights=vals, minlength=R)
-    s2 = np.bincount(idx[n], weights=vals * vals, minlength=R)
-    mean = s1 * inv
-    F = 3 + 3 * (N - 1) + N
+
+    def row_mean(w):
+        return np.bincount(idx[n], weights=w, minlength=R) * inv
+
+    mean = row_mean(vals)
+    D = N - 1
+    F = 4 + 6 * D + N
     out = np.zeros((R, F))
     out[:, 0] = np.log1p(c)
     out[:, 1] = mean
-    out[:, 2] = np.sqrt(np.maximum(0.0, s2 * inv - mean * mean))
+    out[:, 2] = np.sqrt(np.maximum(0.0, row_mean(vals * vals) - mean * mean))
+    prod = vals.copy()
     d = 0
     for m in range(N):
         if m == n:
             continue
         a = mu[m][idx[m]]
         b = lc[m][idx[m]]
-        am = np.bincount(idx[n], weights=a, minlength=R) * inv
-        aq = np.bincount(idx[n], weights=a * a, minlength=R) * inv
-        out[:, 3 + 3 * d] = am
-        out[:, 4 + 3 * d] = np.sqrt(np.maximum(0.0, aq - am * am))
-        out[:, 5 + 3 * d] = np.bincount(idx[n], weights=b, minlength=R) * inv
+        am = row_mean(a)
+        out[:, 3 + 6 * d] = am
+        out[:, 4 + 6 * d] = np.sqrt(np.maximum(0.0, row_mean(a * a) - am * am))
+        out[:, 5 + 6 * d] = row_mean(b)
+        out[:, 6 + 6 * d] = row_mean(vals * a)
+        out[:, 7 + 6 * d] = row_mean(vals * a * a)
+        out[:, 8 + 6 * d] = row_mean(vals * b)
+        prod = prod * a
         d += 1
-    out[:, 3 + 3 * (N - 1) + n] = 1.0
+    out[:, 3 + 6 * D] = row_mean(prod)
+    out[:, 4 + 6 * D + n] = 1.0
     return out
 
 

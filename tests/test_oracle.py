@@ -229,6 +229,9 @@ def test_warmstart_oracle_features_by_hand():
     vals = np.array([1.0, 3.0, 5.0])
     f = orc.row_features(idx, vals, [2, 3], 0)
     # row 0 of mode 0: c = 2, values 1, 3 -> mean 2, std 1; co-indexed mode-1 rows 1 (mean 1, c 1)
-    # and 2 (mean 4, c 2): mean 2.5, std 1.5, mean log1p(c) = (log 2 + log 3) / 2; one-hot [1, 0]
-    np.testing.assert_allclose(f[0], [np.log(3), 2, 1, 2.5, 1.5, (np.log(2) + np.log(3)) / 2, 1, 0])
-    np.testing.assert_allclose(f[1], [np.log(2), 5, 0, 4, 0, np.log(3), 1, 0])
+    # and 2 (mean 4, c 2): mean 2.5, std 1.5, mean log1p(c) = (log 2 + log 3) / 2;
+    # E[x mu] = (1*1 + 3*4)/2, E[x mu^2] = (1*1 + 3*16)/2, E[x lc] = (log 2 + 3 log 3)/2;
+    # E[x prod mu] = E[x mu]; one-hot [1, 0]
+    l2, l3 = np.log(2), np.log(3)
+    np.testing.assert_allclose(f[0], [l3, 2, 1, 2.5, 1.5, (l2 + l3) / 2, 6.5, 24.5, (l2 + 3 * l3) / 2, 6.5, 1, 0])
+    np.testing.assert_allclose(f[1], [l2, 5, 0, 4, 0, l3, 20, 80, 5 * l3, 20, 1, 0])
