@@ -318,6 +318,125 @@ template <class V, int KE, bool EXACT> struct GramAcc {
 
 __host__ __device__ constexpr int gram_slots(int J) { return ((J + 1) * (J + 2) / 2 - 1 + 31) / 32; }
 
+// Running Gram/RHS sums of one warp, register-blocked (the tensor-core forms):
+// lane l owns 2 x 2 blocks (rb, cb), rb <= cb, of the (J+1) x (J+1) outer product
+// of [delta, x] (features padded to an even count FP, the pad column zero), loads
+// each operand pair with one 64-bit shared-memory load (the delta tile's row
+// stride is even) and keeps four FP32 partial sums per block and run (4-way
+// unrolled over the run's positions), merged with Neumaier compensation; runs of
+// equal rows come from one ballot per 32 positions, a row change flushes the
+// packed entries (i <= j, not (J, J)) with FP64 atomics.  Same sums as GramAcc's
+// non-exact form, in a different association.
+template <int J> struct GramBlk {
+  static constexpr int FP = (J + 2) / 2 * 2;  // J + 1 features rounded up to even
+  static constexpr int NB2 = FP / 2;
+  static constexpr int NBLK = NB2 * (NB2 + 1) / 2;
+  static constexpr int KB = (NBLK + 31) / 32;
+  ProdSum<float> acc[KB][4];
+  int orow[KB], ocol[KB];  // first feature of the block's row pair / column pair; -1: no block
+  uint32_t row = 0xFFFFFFFFu;
+
+  __device__ void init(int lane) {
+#pragma unroll
+    for (int k = 0; k < KB; ++k) {
+      int b = lane + 32 * k, rb = 0;
+      if (b < NBLK) {
+        while (b >= NB2 - rb) {
+          b -= NB2 - rb;
+          ++rb;
+        }
+        orow[k] = 2 * rb;
+        ocol[k] = 2 * (rb + b);
+      } else {
+        orow[k] = ocol[k] = -1;
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[k][q] = ProdSum<float>();
+    }
+  }
+  __device__ static int entry(int i, int j) { return i * (J + 1) - i * (i - 1) / 2 + (j - i); }
+  __device__ void flush(double *gram, int E, int lane) {
+    if (row != 0xFFFFFFFFu) {
+#pragma unroll
+      for (int k = 0; k < KB; ++k) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = orow[k] + (q >> 1), j = ocol[k] + (q & 1);
+          if (orow[k] >= 0 && i <= j && j <= J && !(i == J && j == J))
+            atomicAdd(gram + (size_t)row * E + entry(i, j), acc[k][q].value());
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < KB; ++k)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[k][q] = ProdSum<float>();
+    (void)lane;
+  }
+  // tile positions [t0, t1) of the shared delta tile (row stride LDD, even; column J = x,
+  // columns J+1 .. FP-1 zero)
+  template <int LDD>
+  __device__ void run(const float *dx, const uint32_t *rows, int t0, int t1, double *gram, int E, int lane) {
+    static_assert(LDD % 2 == 0 && LDD >= FP, "64-bit pair loads");
+    for (int base = t0; base < t1; base += 32) {
+      const int n = min(32, t1 - base);
+      const uint32_t my = lane < n ? rows[base + lane] : 0xFFFFFFFFu;
+      const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, my, 1);
+      const bool head = lane < n && (lane == 0 ? my != row : my != prev);
+      uint32_t heads = __ballot_sync(0xFFFFFFFFu, head);
+      int a = 0;
+      while (a < n) {
+        if (heads & 1u) {
+          flush(gram, E, lane);
+          row = __shfl_sync(0xFFFFFFFFu, my, a);
+        }
+        const uint32_t rest = heads >> 1;
+        const int b = rest ? min(n, a + 1 + __ffs(rest) - 1) : n;
+        float p[KB][4][2];
+#pragma unroll
+        for (int k = 0; k < KB; ++k)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) p[k][q][0] = p[k][q][1] = 0.f;
+        int t = base + a;
+        const int te = base + b;
+        for (; t + 2 <= te; t += 2) {
+#pragma unroll
+          for (int u = 0; u < 2; ++u) {
+            const float *d = dx + (t + u) * LDD;
+#pragma unroll
+            for (int k = 0; k < KB; ++k) {
+              const float2 r = *reinterpret_cast<const float2 *>(d + max(orow[k], 0));
+              const float2 c = *reinterpret_cast<const float2 *>(d + max(ocol[k], 0));
+              p[k][0][u] = fmaf(r.x, c.x, p[k][0][u]);
+              p[k][1][u] = fmaf(r.x, c.y, p[k][1][u]);
+              p[k][2][u] = fmaf(r.y, c.x, p[k][2][u]);
+              p[k][3][u] = fmaf(r.y, c.y, p[k][3][u]);
+            }
+          }
+        }
+        for (; t < te; ++t) {
+          const float *d = dx + t * LDD;
+#pragma unroll
+          for (int k = 0; k < KB; ++k) {
+            const float2 r = *reinterpret_cast<const float2 *>(d + max(orow[k], 0));
+            const float2 c = *reinterpret_cast<const float2 *>(d + max(ocol[k], 0));
+            p[k][0][0] = fmaf(r.x, c.x, p[k][0][0]);
+            p[k][1][0] = fmaf(r.x, c.y, p[k][1][0]);
+            p[k][2][0] = fmaf(r.y, c.x, p[k][2][0]);
+            p[k][3][0] = fmaf(r.y, c.y, p[k][3][0]);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < KB; ++k)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[k][q].add(p[k][q][0] + p[k][q][1]);
+        heads = b - a >= 32 ? 0u : (heads >> (b - a));
+        a = b;
+      }
+    }
+  }
+};
+
 __device__ inline double block_sum(double v) {
   __shared__ double sw[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

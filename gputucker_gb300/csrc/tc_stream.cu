@@ -57,7 +57,7 @@ template <int N, int J> struct TsShape {
   static constexpr int SBO = (KP / 8) * 128;  // bytes between 8-row groups (A and B alike)
   static constexpr int A_BYTES = kTsThreads * KP * 2;
   static constexpr int B_BYTES = CW * KP * 2;  // one chunk
-  static constexpr int LDD = ((J + 2) & 1) ? J + 2 : J + 3;
+  static constexpr int LDD = (J + 2) / 2 * 2;  // even (64-bit pair loads in GramBlk)
   static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
   static constexpr int OFF_B = A_BYTES;
   static constexpr int OFF_OROW = OFF_B + 2 * B_BYTES;
@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
     fence_mbar_init();
   }
   if (KIND == 0) fill_pairs(ts.pi, ts.pj, J);
-  ts.dx[tid * S::LDD + J + 1] = 0.f;
+  for (int c = J + 1; c < S::LDD; ++c) ts.dx[tid * S::LDD + c] = 0.f;
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -141,8 +141,8 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
   constexpr uint32_t IDESC = instr_desc(GTK_PREC_BF16, 128, S::CW);
   const float *facn = reinterpret_cast<const float *>(a.fac[a.mode]);
   double err = 0;
-  GramAcc<float, gram_slots(J), false> gram;
-  if (KIND == 0) gram.init(ts.pi, ts.pj, S::E, J + 1, tid & 31);
+  GramBlk<J> gram;
+  if (KIND == 0) gram.init(tid & 31);
 
   const uint64_t ntiles = (a.nnz + kTsThreads - 1) / kTsThreads;
   const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
@@ -320,7 +320,7 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
         float *dst = reinterpret_cast<float *>(a.dstore) + t0 * J;
         for (int k = tid; k < nv * J; k += kTsThreads) dst[k] = ts.dx[(k / J) * S::LDD + (k % J)];
       }
-      gram.run(ts.dx, S::LDD, ts.rows, warp * 32, min(warp * 32 + 32, nv), a.gram, S::E, tid & 31);
+      gram.template run<S::LDD>(ts.dx, ts.rows, warp * 32, min(warp * 32 + 32, nv), a.gram, S::E, tid & 31);
       __syncthreads();
     } else if (KIND == 1) {
       if (valid) {

@@ -49,7 +49,7 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int SBO = (KP / EPC) * 128;  // bytes between 8-row groups
   static constexpr int A_BYTES = kTcThreads * KP * ES;
   static constexpr int B_BYTES = NP * KP * ES;
-  static constexpr int LDD = ((J + 2) & 1) ? J + 2 : J + 3;  // column J + 1 stays zero
+  static constexpr int LDD = (J + 2) / 2 * 2;  // even (64-bit pair loads in GramBlk); column J + 1 stays zero
   static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
   static constexpr int OFF_B = A_BYTES;
   static constexpr int OFF_DX = (OFF_B + B_BYTES + 15) / 16 * 16;
@@ -113,10 +113,10 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   double err = 0;
   uint32_t phase = 0;
   bool timed_out = false;
-  GramAcc<float, gram_slots(J), false> gram;
-  for (int k = tid; k < kTcThreads; k += kTcThreads) ts.dx[k * S::LDD + J + 1] = 0.f;
+  GramBlk<J> gram;
+  for (int c = J + 1; c < S::LDD; ++c) ts.dx[tid * S::LDD + c] = 0.f;
   __syncthreads();
-  if (KIND == 0) gram.init(ts.pi, ts.pj, S::E, J + 1, tid & 31);
+  if (KIND == 0) gram.init(tid & 31);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
   const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
@@ -237,7 +237,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
         float *dst = reinterpret_cast<float *>(a.dstore) + t0 * J;
         for (int k = tid; k < nv * J; k += kTcThreads) dst[k] = ts.dx[(k / J) * S::LDD + (k % J)];
       }
-      gram.run(ts.dx, S::LDD, ts.rows, warp * 32, min(warp * 32 + 32, nv), a.gram, S::E, tid & 31);
+      gram.template run<S::LDD>(ts.dx, ts.rows, warp * 32, min(warp * 32 + 32, nv), a.gram, S::E, tid & 31);
       __syncthreads();
     } else if (KIND == 1) {
       if (valid) {
