@@ -52,8 +52,11 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int LDD = (J + 2) / 2 * 2;  // even (64-bit pair loads in GramBlk); column J + 1 stays zero
   static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
   static constexpr int OFF_B = A_BYTES;
-  static constexpr int OFF_DX = (OFF_B + B_BYTES + 15) / 16 * 16;
-  static constexpr int OFF_ROWS = OFF_DX + (kTcThreads * LDD * 4 + 15) / 16 * 16;
+  // the delta tile reuses the A tile: it is written only after the tile's MMAs
+  // have completed, and the next A tile only after the reduction has read it
+  static constexpr int OFF_DX = 0;
+  static_assert(kTcThreads * LDD * 4 <= A_BYTES, "delta tile must fit in the A tile");
+  static constexpr int OFF_ROWS = (OFF_B + B_BYTES + 15) / 16 * 16;
   static constexpr int OFF_SEG = OFF_ROWS + kTcThreads * 4;
   static constexpr int OFF_PAIRS = OFF_SEG + ((kTcThreads + 1) * 4 + 15) / 16 * 16;
   static constexpr int OFF_BAR = OFF_PAIRS + (2 * E + 15) / 16 * 16;
@@ -114,8 +117,6 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   uint32_t phase = 0;
   bool timed_out = false;
   GramBlk<J> gram;
-  for (int c = J + 1; c < S::LDD; ++c) ts.dx[tid * S::LDD + c] = 0.f;
-  __syncthreads();
   if (KIND == 0) gram.init(tid & 31);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
@@ -231,6 +232,8 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
 #pragma unroll
       for (int j = 0; j < J; ++j) ts.dx[tid * S::LDD + j] = delta[j];
       ts.dx[tid * S::LDD + J] = x;
+#pragma unroll
+      for (int c = J + 1; c < S::LDD; ++c) ts.dx[tid * S::LDD + c] = 0.f;  // the A tile left data there
       ts.rows[tid] = row;
       __syncthreads();
       if (a.dstore) {  // the tile's delta rows, contiguous in view order
