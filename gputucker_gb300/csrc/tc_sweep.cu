@@ -15,8 +15,15 @@
 // tcgen05.ld, finishes delta in registers and hands it to the same row-segmented
 // Gram/RHS reduction as the plain kernel.
 //
+// One CTA barrier per tile: the A tile is complete for the MMAs, every warp has
+// read its TMEM lanes of the previous tile, and the CTA agrees on whether the
+// previous tile's MMA wait gave up.  Everything after the MMAs is warp-private:
+// warp w's delta rows live inside its own 32 rows of the A tile (free once the
+// MMAs completed) and its Gram/RHS run reads only them.
+//
 // Every wait on the MMA-completion mbarrier is bounded: on timeout the CTA sets
-// bit 1 of the status word, frees its TMEM and returns.
+// bit 1 of the status word, waits (bounded) for the MMAs it issued, frees its
+// TMEM and returns.
 
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -52,10 +59,13 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int LDD = (J + 2) / 2 * 2;  // even (64-bit pair loads in GramBlk); column J + 1 stays zero
   static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
   static constexpr int OFF_B = A_BYTES;
-  // the delta tile reuses the A tile: it is written only after the tile's MMAs
-  // have completed, and the next A tile only after the reduction has read it
+  // warp w's delta rows reuse its own 32 rows of the A tile (a contiguous
+  // 32 * KP * ES bytes in the canonical layout): written only after the tile's
+  // MMAs have completed, overwritten by the next A tile only after the warp's
+  // reduction has read them
   static constexpr int OFF_DX = 0;
-  static_assert(kTcThreads * LDD * 4 <= A_BYTES, "delta tile must fit in the A tile");
+  static constexpr int WARP_A_BYTES = 32 * KP * ES;
+  static_assert(32 * LDD * 4 <= WARP_A_BYTES, "a warp's delta rows must fit in its A rows");
   static constexpr int OFF_ROWS = (OFF_B + B_BYTES + 15) / 16 * 16;
   static constexpr int OFF_SEG = OFF_ROWS + kTcThreads * 4;
   static constexpr int OFF_PAIRS = OFF_SEG + ((kTcThreads + 1) * 4 + 15) / 16 * 16;
@@ -72,11 +82,11 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + S::OFF_BAR);
   uint32_t *slot = reinterpret_cast<uint32_t *>(smem + S::OFF_SLOT);
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   TileSmem<float> ts;
   ts.gp = nullptr;
   ts.arow = nullptr;
-  ts.dx = reinterpret_cast<float *>(smem + S::OFF_DX);
+  ts.dx = reinterpret_cast<float *>(smem + S::OFF_DX + warp * S::WARP_A_BYTES);  // this warp's delta rows
   ts.rows = reinterpret_cast<uint32_t *>(smem + S::OFF_ROWS);
   ts.seg = reinterpret_cast<uint32_t *>(smem + S::OFF_SEG);
   ts.pi = smem + S::OFF_PAIRS;
@@ -115,9 +125,9 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   const float *facn = reinterpret_cast<const float *>(a.fac[a.mode]);
   double err = 0;
   uint32_t phase = 0;
-  bool timed_out = false;
+  bool timed_out = false, late = false;  // late: this thread's last MMA wait gave up
   GramBlk<J> gram;
-  if (KIND == 0) gram.init(tid & 31);
+  if (KIND == 0) gram.init(lane);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
   const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
@@ -180,7 +190,10 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
     }
     fence_proxy_async_smem();
     tc_fence_before();
-    __syncthreads();
+    if (__syncthreads_or(late ? 1 : 0)) {  // the previous tile's wait gave up somewhere in the CTA
+      timed_out = true;
+      break;
+    }
     if (tid == 0) {
       tc_fence_after();
 #pragma unroll
@@ -196,11 +209,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
     bool done = false;
     while (!(done = mbar_try_wait(bar, phase)) && ++spins < kWaitLimit) {
     }
-    timed_out = __syncthreads_or(done ? 0 : 1) != 0;  // the whole CTA agrees
-    if (timed_out) {
-      if (tid == 0) atomicOr(a.status, 2);
-      break;
-    }
+    late = !done;  // voted on at the next barrier; until then the results are discarded anyway
     phase ^= 1u;
     tc_fence_after();
     // epilogue: delta from this thread's TMEM lane
@@ -230,18 +239,19 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
     tc_fence_before();
     if (KIND == 0) {
 #pragma unroll
-      for (int j = 0; j < J; ++j) ts.dx[tid * S::LDD + j] = delta[j];
-      ts.dx[tid * S::LDD + J] = x;
+      for (int j = 0; j < J; ++j) ts.dx[lane * S::LDD + j] = delta[j];
+      ts.dx[lane * S::LDD + J] = x;
 #pragma unroll
-      for (int c = J + 1; c < S::LDD; ++c) ts.dx[tid * S::LDD + c] = 0.f;  // the A tile left data there
+      for (int c = J + 1; c < S::LDD; ++c) ts.dx[lane * S::LDD + c] = 0.f;  // the A tile left data there
       ts.rows[tid] = row;
-      __syncthreads();
-      if (a.dstore) {  // the tile's delta rows, contiguous in view order
-        float *dst = reinterpret_cast<float *>(a.dstore) + t0 * J;
-        for (int k = tid; k < nv * J; k += kTcThreads) dst[k] = ts.dx[(k / J) * S::LDD + (k % J)];
+      __syncwarp();
+      const int nw = max(0, min(32, nv - warp * 32));  // this warp's valid nonzeros
+      if (a.dstore) {  // the warp's delta rows, contiguous in view order
+        float *dst = reinterpret_cast<float *>(a.dstore) + (t0 + warp * 32) * J;
+        for (int k = lane; k < nw * J; k += 32) dst[k] = ts.dx[(k / J) * S::LDD + (k % J)];
       }
-      gram.template run<S::LDD>(ts.dx, ts.rows, warp * 32, min(warp * 32 + 32, nv), a.gram, S::E, tid & 31);
-      __syncthreads();
+      gram.template run<S::LDD>(ts.dx, ts.rows + warp * 32, 0, nw, a.gram, S::E, lane);
+      __syncwarp();  // the next A tile overwrites these rows
     } else if (KIND == 1) {
       if (valid) {
         float xh = 0.f;
@@ -250,18 +260,25 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
         const float d = x - xh;
         err += (double)d * (double)d;
       }
-      __syncthreads();
     } else {
       if (valid) {
         float *out = reinterpret_cast<float *>(a.out) + (size_t)a.vperm[gi] * J;
 #pragma unroll
         for (int j = 0; j < J; ++j) out[j] = delta[j];
       }
-      __syncthreads();
     }
     cur = nxt;
   }
-  if (KIND == 0) gram.flush(a.gram, S::E, tid & 31);
+  // the last tile's wait (a CTA that broke out of the loop agreed already)
+  if (!timed_out && __syncthreads_or(late ? 1 : 0)) timed_out = true;
+  if (timed_out) {
+    if (tid == 0) atomicOr(a.status, 2);
+    // the MMAs of the tile whose wait gave up may still run: wait for them (bounded) before freeing TMEM
+    uint32_t spins = 0;
+    while (!mbar_try_wait(bar, phase ^ 1u) && ++spins < kWaitLimit) {
+    }
+  }
+  if (KIND == 0 && !timed_out) gram.flush(a.gram, S::E, lane);
   if (KIND == 1) {
     const double tot = block_sum(err);
     if (tid == 0) a.partial[blockIdx.x] = tot;
