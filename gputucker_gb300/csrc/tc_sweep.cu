@@ -133,42 +133,60 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
   const uint64_t tile_end = min(ntiles, (uint64_t)(blockIdx.x + 1) * per);
   // inputs of one tile for this thread: its nonzero's row, value and the factor
-  // rows (p, q form the Kronecker operand; e1 (D = 3) finishes the contraction)
+  // rows (p, q form the Kronecker operand; e1 (D = 3) finishes the contraction).
+  // Loaded in two stages a tile apart -- the coordinates two tiles ahead, the
+  // factor rows one tile ahead -- so no gather waits on the load of its own index.
+  struct TileCrd {
+    uint32_t row, ip, iq, ie;
+    float x;
+  };
   struct TileIn {
     uint32_t row;
     float x;
     float p[LDG], q[LDG], e1[LDG];
   };
-  auto load_tile = [&](uint64_t tl, TileIn &in) {
+  auto load_crd = [&](uint64_t tl, TileCrd &c) {
     const uint64_t b0 = tl * kTcThreads;
     const int n_valid = (int)min((uint64_t)kTcThreads, a.nnz - b0);
     const bool ok = tid < n_valid;
     const uint64_t g = ok ? b0 + tid : b0;
-    in.row = ok ? a.coord[a.mode][g] : 0xFFFFFFFFu;
-    in.x = ok ? reinterpret_cast<const float *>(a.val)[g] : 0.f;
+    c.row = ok ? a.coord[a.mode][g] : 0xFFFFFFFFu;
+    c.x = ok ? reinterpret_cast<const float *>(a.val)[g] : 0.f;
+    c.ip = a.coord[a.others[D - 2]][g];
+    c.iq = a.coord[a.others[D - 1]][g];
+    c.ie = D == 3 ? a.coord[a.others[0]][g] : 0u;
+  };
+  auto load_rows = [&](const TileCrd &c, TileIn &in) {
+    in.row = c.row;
+    in.x = c.x;
     const float4 *fp = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 2]]) +
-                                                        (size_t)a.coord[a.others[D - 2]][g] * LDG);
+                                                        (size_t)c.ip * LDG);
     const float4 *fq = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 1]]) +
-                                                        (size_t)a.coord[a.others[D - 1]][g] * LDG);
+                                                        (size_t)c.iq * LDG);
 #pragma unroll
-    for (int c = 0; c < LDG / 4; ++c) {
-      const float4 u = __ldg(fp + c), w = __ldg(fq + c);
-      in.p[4 * c] = u.x, in.p[4 * c + 1] = u.y, in.p[4 * c + 2] = u.z, in.p[4 * c + 3] = u.w;
-      in.q[4 * c] = w.x, in.q[4 * c + 1] = w.y, in.q[4 * c + 2] = w.z, in.q[4 * c + 3] = w.w;
+    for (int k = 0; k < LDG / 4; ++k) {
+      const float4 u = __ldg(fp + k), w = __ldg(fq + k);
+      in.p[4 * k] = u.x, in.p[4 * k + 1] = u.y, in.p[4 * k + 2] = u.z, in.p[4 * k + 3] = u.w;
+      in.q[4 * k] = w.x, in.q[4 * k + 1] = w.y, in.q[4 * k + 2] = w.z, in.q[4 * k + 3] = w.w;
     }
     if (D == 3) {
       const float4 *fe = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[0]]) +
-                                                          (size_t)a.coord[a.others[0]][g] * LDG);
+                                                          (size_t)c.ie * LDG);
 #pragma unroll
-      for (int c = 0; c < LDG / 4; ++c) {
-        const float4 u = __ldg(fe + c);
-        in.e1[4 * c] = u.x, in.e1[4 * c + 1] = u.y, in.e1[4 * c + 2] = u.z, in.e1[4 * c + 3] = u.w;
+      for (int k = 0; k < LDG / 4; ++k) {
+        const float4 u = __ldg(fe + k);
+        in.e1[4 * k] = u.x, in.e1[4 * k + 1] = u.y, in.e1[4 * k + 2] = u.z, in.e1[4 * k + 3] = u.w;
       }
     }
   };
   TileIn cur;
+  TileCrd crd;  // coordinates of the tile after `cur`
   const uint64_t tile_begin = (uint64_t)blockIdx.x * per;
-  if (tile_begin < tile_end) load_tile(tile_begin, cur);
+  if (tile_begin < tile_end) {
+    load_crd(tile_begin, crd);
+    load_rows(crd, cur);
+  }
+  if (tile_begin + 1 < tile_end) load_crd(tile_begin + 1, crd);
   for (uint64_t tile = tile_begin; tile < tile_end; ++tile) {
     const uint64_t t0 = tile * kTcThreads;
     const int nv = (int)min((uint64_t)kTcThreads, a.nnz - t0);
@@ -204,7 +222,8 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
     }
     // the next tile's loads overlap this tile's MMAs, epilogue and reduction
     TileIn nxt;
-    if (tile + 1 < tile_end) load_tile(tile + 1, nxt);
+    if (tile + 1 < tile_end) load_rows(crd, nxt);
+    if (tile + 2 < tile_end) load_crd(tile + 2, crd);
     uint32_t spins = 0;
     bool done = false;
     while (!(done = mbar_try_wait(bar, phase)) && ++spins < kWaitLimit) {
