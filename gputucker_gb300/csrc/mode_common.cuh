@@ -437,6 +437,132 @@ template <int J> struct GramBlk {
   }
 };
 
+// GramMma's delta-row stride: 8 or 24 floats, so that the fragment loads of a warp
+// (rows c, c + 4 of 8, columns g, g + 8) hit 32 distinct banks
+__host__ __device__ constexpr int gram_mma_ldd(int J) { return J + 1 <= 8 ? 8 : 24; }
+
+// One warp's Gram/RHS reduction of its 32 delta rows on the tensor cores, for
+// J + 1 <= 16 features f = [delta, x].  For a run [a, b) of nonzeros of one row,
+// G += F[a:b]^T F[a:b] with mma.sync m16n8k8 (A = F^T masked to the run, B = F):
+// a 16 x 16 (or 16 x 8) block holds the whole (J+1) x (J+1) Gram/RHS triangle,
+// per 8 nonzeros three MMAs per 8-column n-tile: the operands are split into TF32
+// big + small parts (truncations: v = big + small + O(2^-20 |v|)) and the product
+// taken as big*big + big*small + small*big, so the products stay within ~2^-19 of
+// FP32's and the sums (FP32 in the MMA over at most 32 nonzeros) near FP32; runs fold
+// into compensated FP32 sums and flush with FP64 atomics on a row change, like
+// GramBlk.  (The 64/128-lane tcgen05 MMA has no 16-row form for this per-warp,
+// per-row product.)  Lane (g = lane / 4, c = lane % 4) owns the accumulator entries
+// (g [+8], 8 nt + 2c [+1]) of n-tile nt.
+template <int J> struct GramMma {
+  static constexpr int F = J + 1;
+  static_assert(F <= 16, "one 16-row MMA block");
+  static constexpr int NT = F <= 8 ? 1 : 2;  // 8-column n-tiles
+  static constexpr int LDD = gram_mma_ldd(J);
+  static constexpr int COLS = F <= 8 ? 8 : 16;  // columns a row must hold (features, then zeros)
+  ProdSum<float> acc[NT][4];
+  uint32_t row = 0xFFFFFFFFu;
+
+  __device__ void init(int) {}
+  __device__ static int entry(int i, int j) { return i * (J + 1) - i * (i - 1) / 2 + (j - i); }
+  // v = big + small + O(2^-20 |v|), both exact TF32 values (low 13 bits zero)
+  __device__ static void split(float v, uint32_t &big, uint32_t &small) {
+    big = __float_as_uint(v) & 0xFFFFE000u;
+    small = __float_as_uint(v - __uint_as_float(big)) & 0xFFFFE000u;  // the difference is exact
+  }
+  __device__ static void mma(float (&d)[4], uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3, uint32_t b0,
+                             uint32_t b1) {
+    asm("mma.sync.aligned.m16n8k8.row.col.f32.tf32.tf32.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+        "{%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+  }
+  // this lane's row of the delta tile: delta, x, zeros up to COLS (16-byte stores)
+  __device__ static void store_row(float *dx_row, const float (&delta)[J], float x) {
+    float v[COLS];
+#pragma unroll
+    for (int k = 0; k < COLS; ++k) v[k] = k < J ? delta[k] : k == J ? x : 0.f;
+#pragma unroll
+    for (int k = 0; k < COLS; k += 4) *reinterpret_cast<float4 *>(dx_row + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+  }
+  __device__ void flush(double *gram, int E, int lane) {
+    if (row != 0xFFFFFFFFu) {
+      const int g = lane >> 2, c = lane & 3;
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i = g + 8 * (q >> 1), j = 8 * nt + 2 * c + (q & 1);
+          if (i <= j && j <= J && !(i == J && j == J)) atomicAdd(gram + (size_t)row * E + entry(i, j), acc[nt][q].value());
+        }
+    }
+#pragma unroll
+    for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+      for (int q = 0; q < 4; ++q) acc[nt][q] = ProdSum<float>();
+  }
+  // rows k0 .. k0 + 7 of the delta tile, restricted (MASK) to the run [a, b)
+  template <bool MASK>
+  __device__ static void kstep(float (&d)[NT][4], const float *dx, int k0, int a, int b, int g, int c) {
+    const float *r0 = dx + (k0 + c) * LDD + g, *r1 = dx + (k0 + c + 4) * LDD + g;
+    uint32_t h0, l0, h2, l2, h1 = 0, l1 = 0, h3 = 0, l3 = 0;
+    split(r0[0], h0, l0);
+    split(r1[0], h2, l2);
+    if (NT > 1) {
+      split(r0[8], h1, l1);
+      split(r1[8], h3, l3);
+    }
+    // A = F^T of the run's nonzeros only; B = F (its other rows meet zeros of A)
+    uint32_t ah0 = h0, ah1 = h1, ah2 = h2, ah3 = h3, al0 = l0, al1 = l1, al2 = l2, al3 = l3;
+    if (MASK) {
+      const bool in0 = (unsigned)(k0 + c - a) < (unsigned)(b - a), in1 = (unsigned)(k0 + c + 4 - a) < (unsigned)(b - a);
+      ah0 = in0 ? h0 : 0u, ah1 = in0 ? h1 : 0u, al0 = in0 ? l0 : 0u, al1 = in0 ? l1 : 0u;
+      ah2 = in1 ? h2 : 0u, ah3 = in1 ? h3 : 0u, al2 = in1 ? l2 : 0u, al3 = in1 ? l3 : 0u;
+    }
+    mma(d[0], ah0, ah1, ah2, ah3, h0, h2);
+    mma(d[0], ah0, ah1, ah2, ah3, l0, l2);
+    mma(d[0], al0, al1, al2, al3, h0, h2);
+    if (NT > 1) {
+      mma(d[NT - 1], ah0, ah1, ah2, ah3, h1, h3);
+      mma(d[NT - 1], ah0, ah1, ah2, ah3, l1, l3);
+      mma(d[NT - 1], al0, al1, al2, al3, h1, h3);
+    }
+  }
+  // rows [0, n) of this warp's delta tile (row stride LDD) with their tensor rows
+  __device__ void run(const float *dx, const uint32_t *rows, int n, double *gram, int E, int lane) {
+    const int g = lane >> 2, c = lane & 3;
+    const uint32_t my = lane < n ? rows[lane] : 0xFFFFFFFFu;
+    const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, my, 1);
+    const bool head = lane < n && (lane == 0 ? my != row : my != prev);
+    uint32_t heads = __ballot_sync(0xFFFFFFFFu, head);
+    int a = 0;
+    while (a < n) {
+      if (heads & 1u) {
+        flush(gram, E, lane);
+        row = __shfl_sync(0xFFFFFFFFu, my, a);
+      }
+      const uint32_t rest = heads >> 1;
+      const int b = rest ? min(n, a + __ffs(rest)) : n;
+      float d[NT][4];
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) d[nt][q] = 0.f;
+      if (b - a == 32) {  // the warp's 32 nonzeros are one row: no masking
+#pragma unroll
+        for (int k0 = 0; k0 < 32; k0 += 8) kstep<false>(d, dx, k0, 0, 32, g, c);
+      } else {
+        for (int k0 = a & ~7; k0 < b; k0 += 8) kstep<true>(d, dx, k0, a, b, g, c);
+      }
+#pragma unroll
+      for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[nt][q].add(d[nt][q]);
+      heads = b - a >= 32 ? 0u : (heads >> (b - a));
+      a = b;
+    }
+  }
+};
+
 __device__ inline double block_sum(double v) {
   __shared__ double sw[32];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

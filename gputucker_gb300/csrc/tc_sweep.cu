@@ -31,6 +31,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
@@ -56,7 +57,12 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int SBO = (KP / EPC) * 128;  // bytes between 8-row groups
   static constexpr int A_BYTES = kTcThreads * KP * ES;
   static constexpr int B_BYTES = NP * KP * ES;
-  static constexpr int LDD = (J + 2) / 2 * 2;  // even (64-bit pair loads in GramBlk); column J + 1 stays zero
+  // Gram/RHS reduction: on the tensor cores (GramMma) for J + 1 <= 16 features, else GramBlk
+  static constexpr bool GRAM_MMA = J + 1 <= 16;
+  using Gram = std::conditional_t<GRAM_MMA, GramMma<J>, GramBlk<J>>;
+  // delta-tile row stride: GramMma's bank-conflict-free stride, or even for
+  // GramBlk's 64-bit pair loads (column J + 1 zero)
+  static constexpr int LDD = GRAM_MMA ? gram_mma_ldd(J) : (J + 2) / 2 * 2;
   static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
   static constexpr int OFF_B = A_BYTES;
   // warp w's delta rows reuse its own 32 rows of the A tile (a contiguous
@@ -126,7 +132,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   double err = 0;
   uint32_t phase = 0;
   bool timed_out = false, late = false;  // late: this thread's last MMA wait gave up
-  GramBlk<J> gram;
+  typename S::Gram gram;
   if (KIND == 0) gram.init(lane);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
@@ -257,11 +263,15 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
     }
     tc_fence_before();
     if (KIND == 0) {
+      if constexpr (S::GRAM_MMA) {
+        GramMma<J>::store_row(ts.dx + lane * S::LDD, delta, x);
+      } else {
 #pragma unroll
-      for (int j = 0; j < J; ++j) ts.dx[lane * S::LDD + j] = delta[j];
-      ts.dx[lane * S::LDD + J] = x;
+        for (int j = 0; j < J; ++j) ts.dx[lane * S::LDD + j] = delta[j];
+        ts.dx[lane * S::LDD + J] = x;
 #pragma unroll
-      for (int c = J + 1; c < S::LDD; ++c) ts.dx[lane * S::LDD + c] = 0.f;  // the A tile left data there
+        for (int c = J + 1; c < S::LDD; ++c) ts.dx[lane * S::LDD + c] = 0.f;  // the A tile left data there
+      }
       ts.rows[tid] = row;
       __syncwarp();
       const int nw = max(0, min(32, nv - warp * 32));  // this warp's valid nonzeros
@@ -269,7 +279,10 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
         float *dst = reinterpret_cast<float *>(a.dstore) + (t0 + warp * 32) * J;
         for (int k = lane; k < nw * J; k += 32) dst[k] = ts.dx[(k / J) * S::LDD + (k % J)];
       }
-      gram.template run<S::LDD>(ts.dx, ts.rows + warp * 32, 0, nw, a.gram, S::E, lane);
+      if constexpr (S::GRAM_MMA)
+        gram.run(ts.dx, ts.rows + warp * 32, nw, a.gram, S::E, lane);
+      else
+        gram.template run<S::LDD>(ts.dx, ts.rows + warp * 32, 0, nw, a.gram, S::E, lane);
       __syncwarp();  // the next A tile overwrites these rows
     } else if (KIND == 1) {
       if (valid) {
