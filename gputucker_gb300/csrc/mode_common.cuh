@@ -553,10 +553,17 @@ template <int J> struct GramMma {
       } else {
         for (int k0 = a & ~7; k0 < b; k0 += 8) kstep<true>(d, dx, k0, a, b, g, c);
       }
+      if (b < n) {  // the row ends inside this warp's nonzeros: one plain add before its flush
 #pragma unroll
-      for (int nt = 0; nt < NT; ++nt)
+        for (int nt = 0; nt < NT; ++nt)
 #pragma unroll
-        for (int q = 0; q < 4; ++q) acc[nt][q].add(d[nt][q]);
+          for (int q = 0; q < 4; ++q) acc[nt][q].s += d[nt][q];
+      } else {      // the row may go on for many tiles: compensated
+#pragma unroll
+        for (int nt = 0; nt < NT; ++nt)
+#pragma unroll
+          for (int q = 0; q < 4; ++q) acc[nt][q].add(d[nt][q]);
+      }
       heads = b - a >= 32 ? 0u : (heads >> (b - a));
       a = b;
     }
