@@ -72,7 +72,7 @@ static void release(DevTensor &t) {
 
 // slab layout [rows][J] <-> device [rows][ldf]
 static int put_factor(DevTensor &t, int n, const void *slabs) {
-  t.fit_from_store = false;
+  fit_invalidate(t);
   GTK_CUDA(cudaMemcpy2DAsync(t.fac[n], (size_t)t.ldf * t.vsize, slabs, (size_t)t.J * t.vsize, (size_t)t.J * t.vsize,
                              t.rows[n], cudaMemcpyHostToDevice, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
@@ -87,7 +87,7 @@ static int get_factor(const DevTensor &t, int n, void *slabs) {
 }
 
 static int put_core(DevTensor &t, const void *core) {
-  t.fit_from_store = false;
+  fit_invalidate(t);
   GTK_CUDA(cudaMemcpyAsync(t.core, core, t.core_n * t.vsize, cudaMemcpyHostToDevice, t.stream));
   if (int rc = upload_core_perms(t, core)) return rc;
   t.have_core = true;
@@ -486,7 +486,7 @@ int gtk_set_precision(gtk_tensor *t, int precision) {
   if (!t) return fail(GTK_ERR_ARG, "null tensor");
   if (precision != GTK_PREC_PLAIN && precision != GTK_PREC_BF16 && precision != GTK_PREC_TF32)
     return fail(GTK_ERR_ARG, "unknown precision");
-  t->fit_from_store = false;
+  fit_invalidate(*t);
   drop_graph(*t);
   if (precision != GTK_PREC_PLAIN && !tc_supported(t->N, t->J, t->dtype, precision))
     return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this order/rank/value type/precision (FP32; "

@@ -172,7 +172,7 @@ int gtk_set_kernel_variant(gtk_tensor *t, int variant) {
   if (variant == GTK_VARIANT_TENSOR_CORE && t->precision == GTK_PREC_PLAIN)
     return fail(GTK_ERR_UNSUPPORTED, "the tensor-core variant needs a precision form (gtk_set_precision)");
   t->variant = variant;
-  t->fit_from_store = false;
+  fit_invalidate(*t);
   drop_graph(*t);
   return 0;
 }
@@ -241,7 +241,7 @@ int gtk_autotune(gtk_tensor *t, int *variant) {
       g_tune_cache[key] = best;
     }
     t->variant = best;
-    t->fit_from_store = false;
+    fit_invalidate(*t);
     drop_graph(*t);
     if (variant) *variant = best;
     return 0;
@@ -300,7 +300,8 @@ int gtk_batch_sweep(gtk_batch *b, double *fits) {
     }
     if (!b->warmed) {
       for (gtk_tensor *t : b->ts)
-        if (int rc = ensure_dstore(*t)) return rc;
+        if (sweep_needs_dstore(*t))
+          if (int rc = ensure_dstore(*t)) return rc;
       if (int rc = batch_enqueue(b)) return rc;
       b->warmed = true;
     } else {
@@ -308,7 +309,7 @@ int gtk_batch_sweep(gtk_batch *b, double *fits) {
         if (int rc = capture(b)) return rc;
       GTK_CUDA(cudaGraphLaunch(b->gexec, b->stream));
     }
-    for (gtk_tensor *t : b->ts) t->fit_from_store = t->dstore != nullptr;
+    for (gtk_tensor *t : b->ts) fit_after_sweep(*t);
     GTK_CUDA(cudaMemcpyAsync(b->h_out.data(), b->d_out, b->h_out.size(), cudaMemcpyDeviceToHost, b->stream));
     GTK_CUDA(cudaStreamSynchronize(b->stream));
     const double *err = reinterpret_cast<const double *>(b->h_out.data());

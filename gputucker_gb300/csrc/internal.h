@@ -138,6 +138,7 @@ struct DevTensor {
   int num_sms = 0;
   uint64_t lu_fallbacks = 0;
   bool fit_from_store = false;  // dstore holds the delta of the last mode's update
+  bool fit_from_gram = false;   // gram holds the last mode's Gram/RHS and fac[N-1] its solution
   bool dstore_failed = false;
   void *dstore = nullptr;       // [nnz][J] value_t, view order of the last mode
   uint32_t *fallback = nullptr; // rows re-solved by pivoted LU
@@ -176,6 +177,9 @@ int run_fit_enqueue(DevTensor &t);
 double fit_from_err(const DevTensor &t, double err);  // fit = 1 - sqrt(err) / ||X|| (the variant's formula)  // the fit kernels only; the sum lands in partial[kFitSumSlot]
 int run_row_stats(DevTensor &t, int mode, uint32_t *max_count);
 int ensure_dstore(DevTensor &t);
+void fit_invalidate(DevTensor &t);         // factors, core or kernel changed: the next fit recomputes
+void fit_after_sweep(DevTensor &t);        // what a replayed sweep leaves for its fit
+bool sweep_needs_dstore(const DevTensor &t);  // a sweep's fit (or its variant) reads the delta store
 void drop_graph(DevTensor &t);
 // tc_sweep.cu: the tensor-core (BF16 / TF32) form; kind 0 update, 1 fit, 2 delta
 // tensor-core form exists for (N, J, value type, precision): tc_sweep.cu's kernels

@@ -848,6 +848,34 @@ __global__ void k_fit_stored(const V *__restrict__ dstore, const uint32_t *__res
   if (threadIdx.x == 0) partial[blockIdx.x] = tot;
 }
 
+// The fit from the last mode's Gram/RHS, without a pass over the nonzeros: with
+// G_i = sum delta delta^T and c_i = sum x delta over row i's nonzeros and a_i the
+// row's new factor row,
+//   sum_{nonzeros of row i} (x - delta . a_i)^2 = sum x^2 - 2 a_i . c_i + a_i^T G_i a_i,
+// so err = ||X||^2 - sum_i (2 a_i . c_i - a_i^T G_i a_i).  Per CTA the negated
+// row sum (CTA 0 adds ||X||^2), so that k_sum_fit yields err.  Gram layout:
+// entry (i, j), i <= j <= J, at i (J+1) - i (i-1) / 2 + (j - i); column J is c.
+template <class V>
+__global__ void k_fit_gram(const double *__restrict__ gram, const V *__restrict__ fac, uint64_t rows, int J, int E,
+                           int ldf, double normsq, double *__restrict__ partial) {
+  double s = 0;
+  for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += (uint64_t)gridDim.x * blockDim.x) {
+    const double *g = gram + r * (uint64_t)E;
+    const V *a = fac + r * (uint64_t)ldf;
+    double q = 0;
+    int e = 0;
+    for (int i = 0; i < J; ++i) {
+      const double ai = (double)a[i];
+      double t = 0.5 * g[e++] * ai;  // the diagonal once, the off-diagonal twice
+      for (int j = i + 1; j < J; ++j) t += g[e++] * (double)a[j];
+      q += ai * (2.0 * g[e++] - 2.0 * t);  // 2 a_i c_i - a_i (G a)_i, upper triangle
+    }
+    s += q;
+  }
+  const double tot = block_sum(s);
+  if (threadIdx.x == 0) partial[blockIdx.x] = (blockIdx.x == 0 ? normsq : 0.0) - tot;
+}
+
 __global__ void k_sum_fit(const double *__restrict__ partial, int m, double *__restrict__ out) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0;
@@ -1057,23 +1085,41 @@ int ensure_dstore(DevTensor &t) {
   return 0;
 }
 
+// the update runs the tensor-core kernels (the precision forms)
+static bool tc_update(const DevTensor &t) {
+  return t.variant == kVarTc || (t.variant == kVarAuto && t.precision != GTK_PREC_PLAIN);
+}
+
+bool sweep_needs_dstore(const DevTensor &t) { return t.variant == kVarRefOrder || !tc_update(t); }
+
+void fit_invalidate(DevTensor &t) {
+  t.fit_from_store = false;
+  t.fit_from_gram = false;
+}
+
+void fit_after_sweep(DevTensor &t) {
+  t.fit_from_gram = tc_update(t);
+  t.fit_from_store = !t.fit_from_gram && t.dstore != nullptr;
+}
+
 template <class V> static int update_impl(DevTensor &t, int mode) {
   const int E = pairs_for(t.J);
   const int J = t.J;
   const bool last = mode == t.N - 1;
-  // the last mode's pass also stores delta, from which the sweep's fit follows exactly
-  // (the reference-order variant stores it on every mode: its B and C come from it)
+  const bool tc = tc_update(t);
+  // the fit follows from the last mode's pass: in the tensor-core forms from its
+  // Gram/RHS (k_fit_gram), otherwise from delta, which the pass then stores (the
+  // reference-order variant stores it on every mode: its B and C come from it)
   void *dstore = nullptr;
-  if ((last || t.variant == kVarRefOrder) && t.nnz) {
+  if (((last && !tc) || t.variant == kVarRefOrder) && t.nnz) {
     if (int rc = ensure_dstore(t)) return rc;
     dstore = t.dstore;
   }
-  t.fit_from_store = false;
+  fit_invalidate(t);
   cudaEvent_t ev = nullptr;
   if (int rc = prof_begin(t, &ev)) return rc;
   GTK_CUDA(cudaMemsetAsync(t.gram, 0, t.rows[mode] * (uint64_t)E * 8, t.stream));
   if (t.nnz) {
-    const bool tc = t.variant == kVarTc || (t.variant == kVarAuto && t.precision != GTK_PREC_PLAIN);
     if (tc) {
       if (int rc = run_mode_tc(t, mode, 0, dstore, nullptr)) return rc;
     } else if (int rc = launch_mode<V, kUpdate>(t, mode, dstore, nullptr)) {
@@ -1148,6 +1194,7 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
     t.launches += 1;
   }
   t.fit_from_store = dstore != nullptr && last;
+  t.fit_from_gram = tc && last;
   if (int rc = prof_end(t, 1, ev)) return rc;
   return 0;
 }
@@ -1173,7 +1220,14 @@ template <class V> static int fit_enqueue(DevTensor &t) {
     t.fit_from_store = false;  // the store now holds x_hat
     return 0;
   }
-  if (t.fit_from_store && t.nnz) {
+  if (t.fit_from_gram && t.nnz) {
+    const int N = t.N;
+    grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(kFitGridMax, (t.rows[N - 1] + 255) / 256));
+    k_fit_gram<V><<<grid, 256, 0, t.stream>>>(t.gram, (const V *)t.fac[N - 1], t.rows[N - 1], t.J, pairs_for(t.J),
+                                              t.ldf, t.norm * t.norm, t.partial);
+    GTK_CUDA(cudaGetLastError());
+    t.launches += 1;
+  } else if (t.fit_from_store && t.nnz) {
     grid = (int)std::min<uint64_t>(kFitGridMax, (t.nnz + 255) / 256);
     k_fit_stored<V><<<grid, 256, 0, t.stream>>>((const V *)t.dstore, t.vidx[t.N - 1][t.N - 1], (const V *)t.vval[t.N - 1],
                                                 (const V *)t.fac[t.N - 1], t.nnz, t.J, t.ldf, t.partial);
@@ -1245,7 +1299,8 @@ int run_sweep(DevTensor &t, double *fit) {
     return run_fit(t, fit);
   }
   if (!t.gexec) {
-    if (int rc = ensure_dstore(t)) return rc;
+    if (sweep_needs_dstore(t))
+      if (int rc = ensure_dstore(t)) return rc;
     const bool prof = t.prof;
     t.prof = false;
     const uint64_t l0 = t.launches;
@@ -1275,7 +1330,7 @@ int run_sweep(DevTensor &t, double *fit) {
   GTK_CUDA(cudaGraphLaunch(t.gexec, t.stream));
   if (int rc = prof_end(t, 3, ev)) return rc;
   t.launches += t.graph_kernels;
-  t.fit_from_store = t.dstore != nullptr;
+  fit_after_sweep(t);
   return fit_read(t, fit);
 }
 

@@ -781,7 +781,7 @@ int gtk_ws_apply(gtk_ws *m, gtk_tensor *t) {
     if (rc) return rc;
   }
   t->have_factors = true;
-  t->fit_from_store = false;
+  fit_invalidate(*t);
   return 0;
 }
 

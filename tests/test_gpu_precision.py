@@ -61,6 +61,34 @@ def test_tensor_core_sweeps_fit(case, prec):
         assert abs(fit - f64) <= BOUND[prec]["fit"]
 
 
+@pytest.mark.parametrize("prec,case", [(p, c) for p in ("bf16", "tf32") for c in TC_CASES] +
+                         [("bf16", c) for c in TS_CASES],
+                         ids=[f"{p}-{c[0]}" for p in ("bf16", "tf32") for c in TC_CASES] +
+                         [f"bf16-{c[0]}" for c in TS_CASES])
+def test_fit_from_gram_matches_direct_fit(case, prec):
+    """In the tensor-core forms a sweep's fit comes from the last mode's Gram/RHS
+    (err = ||X||^2 - sum_i (2 a_i.c_i - a_i^T G_i a_i)); after the factors are set
+    again the fit kernel recomputes delta and sums (x - x_hat)^2 directly.  Both
+    within 1e-5 (the expansion loses ~||X||^2/err of the Gram sums' ~1e-7)."""
+    name, dims, nnz, P, J, _ = case
+    idx, vals = data(case, 0)
+    with gtk.create_tensor_blocks(gtk.coo_from_arrays(idx, vals, dims=dims), P, J) as t:
+        t.init_random(1, 0)
+        t.set_precision(prec)
+        for s in range(2):
+            t.update_factor_matrices()
+            f_gram = t.reconstruction()
+            t.set_factor(len(dims) - 1, t.get_factor(len(dims) - 1))  # the Gram no longer describes the factors
+            f_direct = t.reconstruction()
+            print(f"{name} {prec} sweep {s}: from Gram {f_gram:.9f} direct {f_direct:.9f}")
+            assert abs(f_gram - f_direct) <= 1e-5 * max(1.0, abs(f_direct)), (s, f_gram, f_direct)
+        # the graph-replayed sweep's fit is the Gram one too
+        t.set_graph(True)
+        f_graph = t.sweep()
+        t.set_factor(0, t.get_factor(0))
+        assert abs(f_graph - t.reconstruction()) <= 1e-5 * max(1.0, abs(f_graph))
+
+
 def test_precision_rejects_unsupported_shape():
     for ci, prec in ((9, "bf16"), (7, "tf32")):  # N = 2; N = 5 has a BF16 form only
         idx, vals = data(CASES[ci], 0)
