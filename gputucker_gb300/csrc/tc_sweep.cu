@@ -205,10 +205,20 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
 #pragma unroll
     for (int c = 0; c < S::KP / S::EPC; ++c) {
       float v[8];
+      if constexpr (J % 2 == 0) {  // packed FP32x2: k, k + 1 share p[k / J]
 #pragma unroll
-      for (int e = 0; e < S::EPC; ++e) {
-        const int k = c * S::EPC + e;
-        v[e] = k < S::KD ? p[k / J] * q[k % J] : 0.f;
+        for (int e = 0; e < S::EPC; e += 2) {
+          const int k = c * S::EPC + e;
+          float2 m = make_float2(0.f, 0.f);
+          if (k < S::KD) m = __fmul2_rn(make_float2(p[k / J], p[k / J]), make_float2(q[k % J], q[k % J + 1]));
+          v[e] = m.x, v[e + 1] = m.y;
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < S::EPC; ++e) {
+          const int k = c * S::EPC + e;
+          v[e] = k < S::KD ? p[k / J] * q[k % J] : 0.f;
+        }
       }
       *reinterpret_cast<uint4 *>(smem + canon_off(tid, c * S::EPC, S::SBO, S::ES)) = pack16<PREC>(v);
     }
@@ -247,16 +257,35 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
       for (int c = 0; c < S::NP / 16; ++c)
         tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c * 16), v[c]);
       tmem_wait_ld();
+      if constexpr (D == 3 && J % 2 == 0) {
+        // packed FP32x2: columns (j_n, j_1), (j_n, j_1 + 1) against e1[j_1], e1[j_1 + 1]
+        float2 acc[J];
 #pragma unroll
-      for (int c = 0; c < S::NP / 16; ++c) {
+        for (int j = 0; j < J; ++j) acc[j] = make_float2(0.f, 0.f);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) {
-          const int col = c * 16 + i;
-          if (col < S::ND) {
-            if (D == 2)
-              delta[col] = v[c][i];
-            else
-              delta[col / J] += cur.e1[col % J] * v[c][i];
+        for (int c = 0; c < S::NP / 16; ++c) {
+#pragma unroll
+          for (int i = 0; i < 16; i += 2) {
+            const int col = c * 16 + i;
+            if (col < S::ND)
+              acc[col / J] = __ffma2_rn(make_float2(cur.e1[col % J], cur.e1[col % J + 1]),
+                                        make_float2(v[c][i], v[c][i + 1]), acc[col / J]);
+          }
+        }
+#pragma unroll
+        for (int j = 0; j < J; ++j) delta[j] = acc[j].x + acc[j].y;
+      } else {
+#pragma unroll
+        for (int c = 0; c < S::NP / 16; ++c) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const int col = c * 16 + i;
+            if (col < S::ND) {
+              if (D == 2)
+                delta[col] = v[c][i];
+              else
+                delta[col / J] += cur.e1[col % J] * v[c][i];
+            }
           }
         }
       }
