@@ -12,8 +12,9 @@
 // K-adjacent core matrices 128 B apart, 8-row groups K*2 B / K*4 B apart).  One
 // thread issues the MMAs (K/16 of them for BF16, K/8 for TF32) into a TMEM
 // accumulator of 128 lanes x N columns; each warp reads its 32 lanes back with
-// tcgen05.ld, finishes delta in registers and hands it to the same row-segmented
-// Gram/RHS reduction as the plain kernel.
+// tcgen05.ld, finishes delta in registers and reduces its 32 rows of [delta, x]
+// into the rows' Gram/RHS (GramMma: mma.sync 3xTF32 per row run; GramBlk for
+// J = 16).
 //
 // One CTA barrier per tile: the A tile is complete for the MMAs, every warp has
 // read its TMEM lanes of the previous tile, and the CTA agrees on whether the
