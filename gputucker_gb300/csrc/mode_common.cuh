@@ -438,13 +438,15 @@ template <int J> struct GramBlk {
 };
 
 // GramMma's delta-row stride: 8 or 24 floats, so that the fragment loads of a warp
-// (rows c, c + 4 of 8, columns g, g + 8) hit 32 distinct banks
+// (rows c, c + 4 of 8, columns g, g + 8, g + 16) hit 32 distinct banks
 __host__ __device__ constexpr int gram_mma_ldd(int J) { return J + 1 <= 8 ? 8 : 24; }
 
 // One warp's Gram/RHS reduction of its 32 delta rows on the tensor cores, for
-// J + 1 <= 16 features f = [delta, x].  For a run [a, b) of nonzeros of one row,
-// G += F[a:b]^T F[a:b] with mma.sync m16n8k8 (A = F^T masked to the run, B = F):
-// a 16 x 16 (or 16 x 8) block holds the whole (J+1) x (J+1) Gram/RHS triangle,
+// J <= 16 (features f = [delta, x]).  For a run [a, b) of nonzeros of one row,
+// G += F[:16, a:b] F[a:b] with mma.sync m16n8k8 (A = the first 16 features of
+// F^T, masked to the run; B = F): a 16 x 8 NT block (NT = ceil((J+1)/8) 8-column
+// n-tiles) holds the whole Gram/RHS triangle (row J = x is needed only at (J, J),
+// which the Gram/RHS does not keep),
 // per 8 nonzeros three MMAs per 8-column n-tile: the operands are split into TF32
 // big + small parts (truncations: v = big + small + O(2^-20 |v|)) and the product
 // taken as big*big + big*small + small*big, so the products stay within ~2^-19 of
@@ -455,10 +457,11 @@ __host__ __device__ constexpr int gram_mma_ldd(int J) { return J + 1 <= 8 ? 8 : 
 // (g [+8], 8 nt + 2c [+1]) of n-tile nt.
 template <int J> struct GramMma {
   static constexpr int F = J + 1;
-  static_assert(F <= 16, "one 16-row MMA block");
-  static constexpr int NT = F <= 8 ? 1 : 2;  // 8-column n-tiles
+  static_assert(J <= 16, "delta in the 16 rows of one MMA block");
+  static constexpr int NT = (F + 7) / 8;  // 8-column n-tiles
   static constexpr int LDD = gram_mma_ldd(J);
-  static constexpr int COLS = F <= 8 ? 8 : 16;  // columns a row must hold (features, then zeros)
+  static constexpr int COLS = 8 * NT;  // columns a row must hold (features, then zeros)
+  static_assert(COLS <= LDD, "row stride");
   ProdSum<float> acc[NT][4];
   uint32_t row = 0xFFFFFFFFu;
 
@@ -504,12 +507,16 @@ template <int J> struct GramMma {
   template <bool MASK>
   __device__ static void kstep(float (&d)[NT][4], const float *dx, int k0, int a, int b, int g, int c) {
     const float *r0 = dx + (k0 + c) * LDD + g, *r1 = dx + (k0 + c + 4) * LDD + g;
-    uint32_t h0, l0, h2, l2, h1 = 0, l1 = 0, h3 = 0, l3 = 0;
+    uint32_t h0, l0, h2, l2, h1 = 0, l1 = 0, h3 = 0, l3 = 0, h4 = 0, l4 = 0, h5 = 0, l5 = 0;
     split(r0[0], h0, l0);
     split(r1[0], h2, l2);
     if (NT > 1) {
       split(r0[8], h1, l1);
       split(r1[8], h3, l3);
+    }
+    if (NT > 2) {  // columns 16 .. 23 (B only)
+      split(r0[16], h4, l4);
+      split(r1[16], h5, l5);
     }
     // A = F^T of the run's nonzeros only; B = F (its other rows meet zeros of A)
     uint32_t ah0 = h0, ah1 = h1, ah2 = h2, ah3 = h3, al0 = l0, al1 = l1, al2 = l2, al3 = l3;
@@ -522,9 +529,14 @@ template <int J> struct GramMma {
     mma(d[0], ah0, ah1, ah2, ah3, l0, l2);
     mma(d[0], al0, al1, al2, al3, h0, h2);
     if (NT > 1) {
-      mma(d[NT - 1], ah0, ah1, ah2, ah3, h1, h3);
-      mma(d[NT - 1], ah0, ah1, ah2, ah3, l1, l3);
-      mma(d[NT - 1], al0, al1, al2, al3, h1, h3);
+      mma(d[1 % NT], ah0, ah1, ah2, ah3, h1, h3);
+      mma(d[1 % NT], ah0, ah1, ah2, ah3, l1, l3);
+      mma(d[1 % NT], al0, al1, al2, al3, h1, h3);
+    }
+    if (NT > 2) {
+      mma(d[2 % NT], ah0, ah1, ah2, ah3, h4, h5);
+      mma(d[2 % NT], ah0, ah1, ah2, ah3, l4, l5);
+      mma(d[2 % NT], al0, al1, al2, al3, h4, h5);
     }
   }
   // rows [0, n) of this warp's delta tile (row stride LDD) with their tensor rows

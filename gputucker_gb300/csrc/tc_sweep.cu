@@ -13,8 +13,7 @@
 // thread issues the MMAs (K/16 of them for BF16, K/8 for TF32) into a TMEM
 // accumulator of 128 lanes x N columns; each warp reads its 32 lanes back with
 // tcgen05.ld, finishes delta in registers and reduces its 32 rows of [delta, x]
-// into the rows' Gram/RHS (GramMma: mma.sync 3xTF32 per row run; GramBlk for
-// J = 16).
+// into the rows' Gram/RHS (GramMma: mma.sync 3xTF32 per row run).
 //
 // One CTA barrier per tile: the A tile is complete for the MMAs, every warp has
 // read its TMEM lanes of the previous tile, and the CTA agrees on whether the
@@ -58,8 +57,8 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int SBO = (KP / EPC) * 128;  // bytes between 8-row groups
   static constexpr int A_BYTES = kTcThreads * KP * ES;
   static constexpr int B_BYTES = NP * KP * ES;
-  // Gram/RHS reduction: on the tensor cores (GramMma) for J + 1 <= 16 features, else GramBlk
-  static constexpr bool GRAM_MMA = J + 1 <= 16;
+  // Gram/RHS reduction: on the tensor cores (GramMma) for J <= 16, else GramBlk
+  static constexpr bool GRAM_MMA = J <= 16;
   using Gram = std::conditional_t<GRAM_MMA, GramMma<J>, GramBlk<J>>;
   // delta-tile row stride: GramMma's bank-conflict-free stride, or even for
   // GramBlk's 64-bit pair loads (column J + 1 zero)
