@@ -279,6 +279,89 @@ __global__ void k_gather_blocks(Ptrs g, const V *__restrict__ val, int N, Dims d
   }
 }
 
+// A nonzero as one 32-byte record: global coordinates in words 0 .. N-1 (N <= 5),
+// the block id in word 5 (block order only), the value's bits in words 6 (FP32)
+// or 6-7 (FP64).  A gather by permutation then reads one DRAM sector per nonzero
+// instead of one per coordinate array and one for the value.
+constexpr int kRecMaxOrder = 5;
+__device__ __forceinline__ void rec_load(const uint4 *__restrict__ rec, uint64_t i, uint32_t (&w)[8]) {
+  const uint4 a = __ldg(rec + 2 * i), b = __ldg(rec + 2 * i + 1);
+  w[0] = a.x, w[1] = a.y, w[2] = a.z, w[3] = a.w, w[4] = b.x, w[5] = b.y, w[6] = b.z, w[7] = b.w;
+}
+__device__ __forceinline__ void rec_store(uint4 *__restrict__ rec, uint64_t i, const uint32_t (&w)[8]) {
+  rec[2 * i] = make_uint4(w[0], w[1], w[2], w[3]);
+  rec[2 * i + 1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
+template <class V> __device__ __forceinline__ void rec_put_val(uint32_t (&w)[8], V v) {
+  if (sizeof(V) == 4) {
+    w[6] = __float_as_uint((float)v);
+  } else {
+    const unsigned long long u = __double_as_longlong((double)v);
+    w[6] = (uint32_t)u, w[7] = (uint32_t)(u >> 32);
+  }
+}
+template <class V> __device__ __forceinline__ V rec_get_val(const uint32_t (&w)[8]) {
+  if (sizeof(V) == 4) return (V)__uint_as_float(w[6]);
+  return (V)__longlong_as_double((long long)(((unsigned long long)w[7] << 32) | w[6]));
+}
+
+// input-order records from the uploaded coordinate arrays and values
+template <class V>
+__global__ void k_pack_records(Ptrs g, const V *__restrict__ val, int N, uint64_t n, uint4 *__restrict__ rec) {
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < kRecMaxOrder; ++k)
+      if (k < N) w[k] = g.p[k][t];
+    rec_put_val<V>(w, val[t]);
+    rec_store(rec, t, w);
+  }
+}
+
+// k_gather_blocks from records; also writes the block-order records (with block id)
+template <class V>
+__global__ void k_gather_blocks_rec(const uint4 *__restrict__ rin, int N, Dims dm, uint64_t n,
+                                    const uint32_t *__restrict__ perm, const uint32_t *__restrict__ sbid, MPtrs gblk,
+                                    MPtrs lidx, V *__restrict__ oval, uint4 *__restrict__ rblk) {
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t w[8];
+    rec_load(rin, perm[p], w);
+    const uint32_t bid = sbid[p];
+    uint32_t b = bid;
+#pragma unroll
+    for (int k = kRecMaxOrder - 1; k >= 0; --k) {
+      if (k < N) {
+        const uint32_t c = b % dm.P[k];
+        b /= dm.P[k];
+        gblk.p[k][p] = w[k];
+        lidx.p[k][p] = w[k] - c * dm.bd[k];
+      }
+    }
+    oval[p] = rec_get_val<V>(w);
+    w[5] = bid;
+    rec_store(rblk, p, w);
+  }
+}
+
+// k_gather_view from block-order records, fused with the where-sort's keys
+// (block id of each view element) and values (its block-order position)
+template <class V>
+__global__ void k_gather_view_rec(const uint32_t *__restrict__ perm, uint64_t n, int N, const uint4 *__restrict__ rblk,
+                                  MPtrs vidx, V *__restrict__ vval, uint32_t *__restrict__ keys,
+                                  uint32_t *__restrict__ vals) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t p = perm[i];
+    uint32_t w[8];
+    rec_load(rblk, p, w);
+#pragma unroll
+    for (int k = 0; k < kRecMaxOrder; ++k)
+      if (k < N) vidx.p[k][i] = w[k];
+    vval[i] = rec_get_val<V>(w);
+    keys[i] = w[5];
+    vals[i] = p;
+  }
+}
+
 template <class V>
 __global__ void k_sumsq(const V *__restrict__ v, uint64_t n, double *__restrict__ partial) {
   __shared__ double sw[32];
@@ -413,6 +496,27 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
   max_scan = std::max<uint64_t>(max_scan, t.nblk + 1);
   TRY(talloc((void **)&sc.sums, ((max_scan + kScanChunk - 1) / kScanChunk + 1) * 8));
 
+  // 32-byte records (N <= 5): input order, then block order; without room for
+  // them the gathers read the coordinate arrays one by one
+  uint4 *rin = nullptr, *rblk = nullptr;
+  if (N <= kRecMaxOrder && n) {
+    if (cudaMalloc((void **)&rin, n * 32) == cudaSuccess) {
+      tmp.push_back(rin);
+      if (cudaMalloc((void **)&rblk, n * 32) == cudaSuccess) {
+        tmp.push_back(rblk);
+      } else {
+        rblk = nullptr;
+      }
+    } else {
+      rin = nullptr;
+    }
+    cudaGetLastError();
+    if (!rblk) rin = nullptr;
+    if (rin) {
+      k_pack_records<V><<<G, T, 0, s>>>(gin, dval, N, n, rin);
+      TRY(ck(cudaGetLastError(), "k_pack_records"));
+    }
+  }
   uint32_t *sbid, *perm;
   TRY(talloc((void **)&sbid, n * 4));
   TRY(talloc((void **)&perm, n * 4));
@@ -434,7 +538,10 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
     TRY(talloc((void **)&gblk.p[k], n * 4));
     lidx.p[k] = t.blk_idx[k];
   }
-  if (n) {
+  if (n && rblk) {
+    k_gather_blocks_rec<V><<<G, T, 0, s>>>(rin, N, dm, n, perm, sbid, gblk, lidx, (V *)t.blk_val, rblk);
+    TRY(ck(cudaGetLastError(), "k_gather_blocks_rec"));
+  } else if (n) {
     k_gather_blocks<V><<<G, T, 0, s>>>(gin, dval, N, dm, n, perm, sbid, gblk, lidx, (V *)t.blk_val);
     TRY(ck(cudaGetLastError(), "k_gather_blocks"));
   }
@@ -461,9 +568,11 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
     TRY(radix_sort(keys, t.vperm[m], n, bits_for(t.dims[m] - 1), sc, s));
     MPtrs vi;
     for (int k = 0; k < N; ++k) vi.p[k] = t.vidx[m][k];
-    if (n) {
+    // where_nnz: stable sort of the view by block id -> (block, row, position)
+    if (n && rblk) {
+      k_gather_view_rec<V><<<G, T, 0, s>>>(t.vperm[m], n, N, rblk, vi, (V *)t.vval[m], keys, perm);
+    } else if (n) {
       k_gather_view<V><<<G, T, 0, s>>>(t.vperm[m], n, N, gb, vi, (const V *)t.blk_val, (V *)t.vval[m]);
-      // where_nnz: stable sort of the view by block id -> (block, row, position)
       k_view_block_keys<<<G, T, 0, s>>>(t.vperm[m], sbid, n, keys, perm);
     }
     TRY(radix_sort(keys, perm, n, bits_for(t.nblk - 1), sc, s));
