@@ -9,7 +9,6 @@
 #include <cstring>
 #include <new>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -42,6 +41,32 @@ int cuda_fail(cudaError_t e, const char *what) {
 }
 
 // Device allocation owned by the handle; honours GTK_DEVICE_MEMORY_CAP (bytes).
+// the reference's norm (tensor_manager.tpp:263-293: NormX += val * val in value_t,
+// input order, sqrt in value_t), summed on the host from the input-order values
+// the partition left on the device; only the reference-order variant uses it
+int ensure_norm_ref(DevTensor &t) {
+  if (t.norm_ref_ready) return 0;
+  if (t.nnz && !t.val_in) return fail(GTK_ERR_STATE, "the input-order values are gone");
+  std::vector<unsigned char> h(t.nnz * t.vsize);
+  if (t.nnz) {
+    GTK_CUDA(cudaMemcpyAsync(h.data(), t.val_in, h.size(), cudaMemcpyDeviceToHost, t.stream));
+    GTK_CUDA(cudaStreamSynchronize(t.stream));
+  }
+  if (t.dtype == GTK_F32) {
+    const float *v = reinterpret_cast<const float *>(h.data());
+    float s = 0.f;
+    for (uint64_t i = 0; i < t.nnz; ++i) s += v[i] * v[i];
+    t.norm_ref = (double)std::sqrt(s);
+  } else {
+    const double *v = reinterpret_cast<const double *>(h.data());
+    double s = 0.0;
+    for (uint64_t i = 0; i < t.nnz; ++i) s += v[i] * v[i];
+    t.norm_ref = std::sqrt(s);
+  }
+  t.norm_ref_ready = true;
+  return 0;
+}
+
 int dalloc(DevTensor &t, void **p, size_t bytes) {
   if (bytes < 16) bytes = 16;
   bytes = (bytes + 255) / 256 * 256;
@@ -321,21 +346,7 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
     if ((rc = ck(cudaMemsetAsync(t->corep[n], 0, (core_n / rank) * t->ldf * vs, t->stream), "memset"))) return bail(rc);
   }
   if ((rc = ck(cudaMemsetAsync(t->status, 0, 16, t->stream), "memset"))) return bail(rc);
-  // the reference's norm (tensor_manager.tpp:263-293: NormX += val * val in value_t,
-  // input order, sqrt in value_t) on a host thread while the GPU partitions
-  std::thread norm_thread([t, coo]() {
-    if (coo->dtype == GTK_F32) {
-      float s = 0.f;
-      for (float v : coo->vf) s += v * v;
-      t->norm_ref = (double)std::sqrt(s);
-    } else {
-      double s = 0.0;
-      for (double v : coo->vd) s += v * v;
-      t->norm_ref = std::sqrt(s);
-    }
-  });
   rc = build_partition(*t, *coo);
-  norm_thread.join();
   if (rc) return bail(rc);
   *out = t;
   return 0;

@@ -171,6 +171,8 @@ int gtk_set_kernel_variant(gtk_tensor *t, int variant) {
   if (variant < GTK_VARIANT_AUTO || variant > GTK_VARIANT_REFERENCE_ORDER) return fail(GTK_ERR_ARG, "unknown variant");
   if (variant == GTK_VARIANT_TENSOR_CORE && t->precision == GTK_PREC_PLAIN)
     return fail(GTK_ERR_UNSUPPORTED, "the tensor-core variant needs a precision form (gtk_set_precision)");
+  if (variant == GTK_VARIANT_REFERENCE_ORDER)
+    if (int rc = ensure_norm_ref(*t)) return rc;
   t->variant = variant;
   fit_invalidate(*t);
   drop_graph(*t);

@@ -64,23 +64,48 @@ __global__ void k_radix_hist(const uint32_t *__restrict__ keys, uint64_t n, int 
   for (int d = threadIdx.x; d <= (int)mask; d += blockDim.x) hist[(uint64_t)d * ntiles + blockIdx.x] = cnt[d];
 }
 
-// offs[d * ntiles + tile] = absolute output position of the tile's first key of digit d
+// offs[d * ntiles + tile] = absolute output position of the tile's first key of digit d.
+// The tile is first ordered by digit in shared memory (stable: rounds, then warps,
+// then lanes, in key order), so that each digit's keys leave as one contiguous run
+// and the global writes coalesce.
 __global__ void k_radix_scatter(const uint32_t *__restrict__ keys, const uint32_t *__restrict__ vals,
                                 uint32_t *__restrict__ okeys, uint32_t *__restrict__ ovals, uint64_t n, int shift,
                                 uint32_t mask, const uint32_t *__restrict__ offs, uint32_t ntiles) {
-  __shared__ uint32_t running[256];
+  __shared__ uint32_t running[256];  // next tile-local position per digit
+  __shared__ uint32_t lstart[256];   // tile-local start of each digit
   __shared__ uint32_t wcnt[kRsThreads / 32][256];
+  __shared__ uint32_t skey[kRsTile], sval[kRsTile];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  for (int d = tid; d <= (int)mask; d += blockDim.x) running[d] = offs[(uint64_t)d * ntiles + blockIdx.x];
   const uint64_t base = (uint64_t)blockIdx.x * kRsTile;
+  const int nt = (int)min((uint64_t)kRsTile, n - base);  // keys in this tile
+  uint32_t key[kRsRounds], val[kRsRounds];
+  for (int d = tid; d < 256; d += blockDim.x) running[d] = 0;
+  __syncthreads();
+#pragma unroll
+  for (int r = 0; r < kRsRounds; ++r) {
+    const int i = r * kRsThreads + tid;
+    key[r] = i < nt ? keys[base + i] : 0u;
+    val[r] = i < nt ? vals[base + i] : 0u;
+    if (i < nt) atomicAdd(&running[(key[r] >> shift) & mask], 1u);
+  }
+  __syncthreads();
+  if (tid == 0) {  // exclusive scan of the tile's digit counts (at most 256)
+    uint32_t acc = 0;
+    for (int d = 0; d <= (int)mask; ++d) {
+      const uint32_t c = running[d];
+      lstart[d] = acc;
+      running[d] = acc;
+      acc += c;
+    }
+  }
+  __syncthreads();
+#pragma unroll
   for (int r = 0; r < kRsRounds; ++r) {
     for (int k = tid; k < (kRsThreads / 32) * 256; k += blockDim.x) (&wcnt[0][0])[k] = 0;
     __syncthreads();
-    const uint64_t i = base + (uint64_t)r * kRsThreads + tid;
-    const bool valid = i < n;
-    const uint32_t key = valid ? keys[i] : 0u;
-    const uint32_t val = valid ? vals[i] : 0u;
-    const uint32_t d = valid ? ((key >> shift) & mask) : 0xFFFFFFFFu;
+    const int i = r * kRsThreads + tid;
+    const bool valid = i < nt;
+    const uint32_t d = valid ? ((key[r] >> shift) & mask) : 0xFFFFFFFFu;
     const uint32_t peers = __match_any_sync(0xFFFFFFFFu, d);
     const uint32_t lrank = __popc(peers & ((1u << lane) - 1u));
     if (valid && lrank == 0) wcnt[warp][d] = __popc(peers);
@@ -89,7 +114,7 @@ __global__ void k_radix_scatter(const uint32_t *__restrict__ keys, const uint32_
       uint32_t p = running[dd];
 #pragma unroll
       for (int w = 0; w < kRsThreads / 32; ++w) {
-        uint32_t c = wcnt[w][dd];
+        const uint32_t c = wcnt[w][dd];
         wcnt[w][dd] = p;
         p += c;
       }
@@ -97,11 +122,18 @@ __global__ void k_radix_scatter(const uint32_t *__restrict__ keys, const uint32_
     }
     __syncthreads();
     if (valid) {
-      const uint32_t pos = wcnt[warp][d] + lrank;
-      okeys[pos] = key;
-      ovals[pos] = val;
+      const uint32_t lpos = wcnt[warp][d] + lrank;
+      skey[lpos] = key[r];
+      sval[lpos] = val[r];
     }
-    __syncthreads();
+    __syncthreads();  // wcnt is cleared for the next round
+  }
+  for (int j = tid; j < nt; j += blockDim.x) {
+    const uint32_t k = skey[j];
+    const uint32_t d = (k >> shift) & mask;
+    const uint64_t pos = (uint64_t)offs[(uint64_t)d * ntiles + blockIdx.x] + (uint32_t)(j - lstart[d]);
+    okeys[pos] = k;
+    ovals[pos] = sval[j];
   }
 }
 
@@ -416,11 +448,21 @@ __global__ void k_where(const uint32_t *__restrict__ keys, const uint32_t *__res
     where[j] = (uint32_t)(pos[j] - blk_ptr[keys[j]]);
 }
 
-// histogram of (block, local row) into count[b*(bd+1) + row]
+// histogram of (block, local row) into count[b*(bd+1) + row]; one atomic per
+// distinct counter in a warp (heavy rows of a skewed tensor recur within a warp)
 __global__ void k_count_rows(const uint32_t *__restrict__ sbid, const uint32_t *__restrict__ lrow, uint64_t n,
                              uint32_t bd, uint64_t *__restrict__ cnt) {
-  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x)
-    atomicAdd((unsigned long long *)&cnt[(uint64_t)sbid[p] * (bd + 1) + lrow[p]], 1ull);
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  const uint64_t start = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t rounds = (n + stride - 1) / stride;  // the same for every thread: whole warps stay converged
+  const int lane = threadIdx.x & 31;
+  for (uint64_t r = 0; r < rounds; ++r) {
+    const uint64_t p = start + r * stride;
+    const bool valid = p < n;
+    const unsigned long long c = valid ? (uint64_t)sbid[p] * (bd + 1) + lrow[p] : ~0ull;
+    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, c);
+    if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd((unsigned long long *)&cnt[c], (unsigned long long)__popc(peers));
+  }
 }
 
 // after a global exclusive scan: count[b][r] -= blk_ptr[b]
@@ -482,8 +524,9 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
     if (n) TRY(ck(cudaMemcpyAsync(p, coo.idx[k].data(), n * 4, cudaMemcpyHostToDevice, s), "upload coords"));
     gin.p[k] = (const uint32_t *)p;
   }
-  V *dval;
-  TRY(talloc((void **)&dval, n * sizeof(V)));
+  // the values stay on the device in input order: the reference's serial norm sums them in that order
+  TRY(dalloc(t, &t.val_in, n * sizeof(V)));
+  V *dval = reinterpret_cast<V *>(t.val_in);
   if (n) TRY(ck(cudaMemcpyAsync(dval, coo.values(), n * sizeof(V), cudaMemcpyHostToDevice, s), "upload values"));
 
   SortScratch sc;

@@ -1263,6 +1263,8 @@ double fit_from_err(const DevTensor &t, double err) {
 }
 
 static int fit_read(DevTensor &t, double *fit) {
+  if (t.variant == kVarRefOrder)
+    if (int rc = ensure_norm_ref(t)) return rc;
   double err = 0;
   GTK_CUDA(cudaMemcpyAsync(&err, t.partial + kFitGridMax, 8, cudaMemcpyDeviceToHost, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
