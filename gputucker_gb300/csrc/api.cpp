@@ -98,18 +98,10 @@ static void release(DevTensor &t) {
 // slab layout [rows][J] <-> device [rows][ldf]
 static int put_factor(DevTensor &t, int n, const void *slabs) {
   fit_invalidate(t);
-  GTK_CUDA(cudaMemcpy2DAsync(t.fac[n], (size_t)t.ldf * t.vsize, slabs, (size_t)t.J * t.vsize, (size_t)t.J * t.vsize,
-                             t.rows[n], cudaMemcpyHostToDevice, t.stream));
-  GTK_CUDA(cudaStreamSynchronize(t.stream));
-  return 0;
+  return factor_from_host(t, n, slabs);
 }
 
-static int get_factor(const DevTensor &t, int n, void *slabs) {
-  GTK_CUDA(cudaMemcpy2DAsync(slabs, (size_t)t.J * t.vsize, t.fac[n], (size_t)t.ldf * t.vsize, (size_t)t.J * t.vsize,
-                             t.rows[n], cudaMemcpyDeviceToHost, t.stream));
-  GTK_CUDA(cudaStreamSynchronize(t.stream));
-  return 0;
-}
+static int get_factor(const DevTensor &t, int n, void *slabs) { return factor_to_host(t, n, slabs); }
 
 static int put_core(DevTensor &t, const void *core) {
   fit_invalidate(t);
@@ -340,6 +332,7 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
   A((void **)&t->fallback, max_rows * 4);
   A((void **)&t->fallback64, max_rows * 4);
   A((void **)&t->nfallback, 16);
+  A(&t->xfer, max_rows * (uint64_t)rank * vs);
   if (rc) return bail(rc);
   for (int n = 0; n < N; ++n) {
     if ((rc = ck(cudaMemsetAsync(t->fac[n], 0, t->rows[n] * t->ldf * vs, t->stream), "memset"))) return bail(rc);

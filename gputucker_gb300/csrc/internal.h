@@ -118,6 +118,7 @@ struct DevTensor {
   double norm_ref = 0;  // the reference's ||X||: value_t serial sum of x^2 in input order, sqrt in value_t
   bool norm_ref_ready = false;  // norm_ref is summed when the reference-order variant is first selected
   void *val_in = nullptr;       // the values in input order (the order of that sum)
+  void *xfer = nullptr;         // [max rows][J] value_t: factors in the slab layout on their way to/from the host
   int precision = GTK_PREC_PLAIN;
   bool have_factors = false, have_core = false;
 
@@ -180,6 +181,8 @@ double fit_from_err(const DevTensor &t, double err);  // fit = 1 - sqrt(err) / |
 int run_row_stats(DevTensor &t, int mode, uint32_t *max_count);
 int ensure_dstore(DevTensor &t);
 int ensure_norm_ref(DevTensor &t);  // the reference's value_t norm from val_in (host, serial)
+int factor_to_host(const DevTensor &t, int n, void *slabs);    // device [rows][ldf] -> host [rows][J]
+int factor_from_host(DevTensor &t, int n, const void *slabs);  // host [rows][J] -> device [rows][ldf]
 void fit_invalidate(DevTensor &t);         // factors, core or kernel changed: the next fit recomputes
 void fit_after_sweep(DevTensor &t);        // what a replayed sweep leaves for its fit
 bool sweep_needs_dstore(const DevTensor &t);  // a sweep's fit (or its variant) reads the delta store

@@ -1336,6 +1336,46 @@ int run_sweep(DevTensor &t, double *fit) {
   return fit_read(t, fit);
 }
 
+// factors between the device layout [rows][ldf] and the reference's slab layout
+// [rows][J]: repacked on the device so that the host copy is one contiguous
+// transfer (a pitched copy of 100,000 rows of 40 bytes runs far below the link)
+template <class V> __global__ void k_fac_pack(const V *__restrict__ fac, uint64_t rows, int J, int ldf, V *__restrict__ out) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows * J; i += (uint64_t)gridDim.x * blockDim.x)
+    out[i] = fac[(i / J) * ldf + i % J];
+}
+template <class V> __global__ void k_fac_unpack(const V *__restrict__ in, uint64_t rows, int J, int ldf, V *__restrict__ fac) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < rows * J; i += (uint64_t)gridDim.x * blockDim.x)
+    fac[(i / J) * ldf + i % J] = in[i];
+}
+
+int factor_to_host(const DevTensor &t, int n, void *slabs) {
+  const uint64_t m = t.rows[n] * (uint64_t)t.J;
+  if (!m) return 0;
+  const unsigned g = (unsigned)std::min<uint64_t>((m + 255) / 256, (uint64_t)t.num_sms * 8);
+  if (t.dtype == GTK_F32)
+    k_fac_pack<float><<<g, 256, 0, t.stream>>>((const float *)t.fac[n], t.rows[n], t.J, t.ldf, (float *)t.xfer);
+  else
+    k_fac_pack<double><<<g, 256, 0, t.stream>>>((const double *)t.fac[n], t.rows[n], t.J, t.ldf, (double *)t.xfer);
+  GTK_CUDA(cudaGetLastError());
+  GTK_CUDA(cudaMemcpyAsync(slabs, t.xfer, m * t.vsize, cudaMemcpyDeviceToHost, t.stream));
+  GTK_CUDA(cudaStreamSynchronize(t.stream));
+  return 0;
+}
+
+int factor_from_host(DevTensor &t, int n, const void *slabs) {
+  const uint64_t m = t.rows[n] * (uint64_t)t.J;
+  if (!m) return 0;
+  GTK_CUDA(cudaMemcpyAsync(t.xfer, slabs, m * t.vsize, cudaMemcpyHostToDevice, t.stream));
+  const unsigned g = (unsigned)std::min<uint64_t>((m + 255) / 256, (uint64_t)t.num_sms * 8);
+  if (t.dtype == GTK_F32)
+    k_fac_unpack<float><<<g, 256, 0, t.stream>>>((const float *)t.xfer, t.rows[n], t.J, t.ldf, (float *)t.fac[n]);
+  else
+    k_fac_unpack<double><<<g, 256, 0, t.stream>>>((const double *)t.xfer, t.rows[n], t.J, t.ldf, (double *)t.fac[n]);
+  GTK_CUDA(cudaGetLastError());
+  GTK_CUDA(cudaStreamSynchronize(t.stream));
+  return 0;
+}
+
 int run_delta(DevTensor &t, int mode, void *d_out) {
   if (!t.nnz) return 0;
   if (t.precision != GTK_PREC_PLAIN) return run_mode_tc(t, mode, 2, d_out, nullptr);
