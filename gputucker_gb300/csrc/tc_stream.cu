@@ -63,9 +63,7 @@ template <int N, int J> struct TsShape {
   static constexpr int OFF_OROW = OFF_B + 2 * B_BYTES;
   static constexpr int OFF_DX = OFF_OROW + (D == 4 ? J * kTsThreads * 4 : 0);
   static constexpr int OFF_ROWS = OFF_DX + (kTsThreads * LDD * 4 + 15) / 16 * 16;
-  static constexpr int OFF_SEG = OFF_ROWS + kTsThreads * 4;
-  static constexpr int OFF_PAIRS = OFF_SEG + ((kTsThreads + 1) * 4 + 15) / 16 * 16;
-  static constexpr int OFF_BAR = OFF_PAIRS + (2 * E + 15) / 16 * 16;  // full[2], done[2]
+  static constexpr int OFF_BAR = OFF_ROWS + (kTsThreads * 4 + 15) / 16 * 16;  // full[2], done[2]
   static constexpr int OFF_SLOT = OFF_BAR + 32;
   static constexpr int SMEM = OFF_SLOT + 16;
   static_assert(B_BYTES % 16 == 0 && OFF_B % 16 == 0 && OFF_OROW % 16 == 0, "16-byte bulk copies");
@@ -119,9 +117,8 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
   ts.arow = nullptr;
   ts.dx = reinterpret_cast<float *>(smem + S::OFF_DX);
   ts.rows = reinterpret_cast<uint32_t *>(smem + S::OFF_ROWS);
-  ts.seg = reinterpret_cast<uint32_t *>(smem + S::OFF_SEG);
-  ts.pi = smem + S::OFF_PAIRS;
-  ts.pj = smem + S::OFF_PAIRS + S::E;
+  ts.seg = nullptr;
+  ts.pi = ts.pj = nullptr;
 
   if (warp == 0) {
     tmem_alloc(slot, 2 * S::NCOLS);
@@ -131,7 +128,6 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
     for (int b = 0; b < 4; ++b) mbar_init(full + b, 1);
     fence_mbar_init();
   }
-  if (KIND == 0) fill_pairs(ts.pi, ts.pj, J);
   for (int c = J + 1; c < S::LDD; ++c) ts.dx[tid * S::LDD + c] = 0.f;
   tc_fence_before();
   __syncthreads();

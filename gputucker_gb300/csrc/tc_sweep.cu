@@ -73,9 +73,7 @@ template <int J, int D, int PREC> struct TcShape {
   static constexpr int WARP_A_BYTES = 32 * KP * ES;
   static_assert(32 * LDD * 4 <= WARP_A_BYTES, "a warp's delta rows must fit in its A rows");
   static constexpr int OFF_ROWS = (OFF_B + B_BYTES + 15) / 16 * 16;
-  static constexpr int OFF_SEG = OFF_ROWS + kTcThreads * 4;
-  static constexpr int OFF_PAIRS = OFF_SEG + ((kTcThreads + 1) * 4 + 15) / 16 * 16;
-  static constexpr int OFF_BAR = OFF_PAIRS + (2 * E + 15) / 16 * 16;
+  static constexpr int OFF_BAR = OFF_ROWS + (kTcThreads * 4 + 15) / 16 * 16;
   static constexpr int OFF_SLOT = OFF_BAR + 16;
   static constexpr int SMEM = OFF_SLOT + 16;
 };
@@ -94,9 +92,8 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   ts.arow = nullptr;
   ts.dx = reinterpret_cast<float *>(smem + S::OFF_DX + warp * S::WARP_A_BYTES);  // this warp's delta rows
   ts.rows = reinterpret_cast<uint32_t *>(smem + S::OFF_ROWS);
-  ts.seg = reinterpret_cast<uint32_t *>(smem + S::OFF_SEG);
-  ts.pi = smem + S::OFF_PAIRS;
-  ts.pj = smem + S::OFF_PAIRS + S::E;
+  ts.seg = nullptr;
+  ts.pi = ts.pj = nullptr;
 
   if (warp == 0) {
     tmem_alloc(slot, S::NCOLS);
@@ -120,7 +117,6 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
       *reinterpret_cast<uint4 *>(smem + S::OFF_B + canon_off(n, c * S::EPC, S::SBO, S::ES)) = pack16<PREC>(v);
     }
   }
-  if (KIND == 0) fill_pairs(ts.pi, ts.pj, J);
   fence_proxy_async_smem();
   tc_fence_before();
   __syncthreads();

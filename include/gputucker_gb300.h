@@ -143,7 +143,11 @@ int gtk_update_mode(gtk_tensor *t, int mode);
 /* replaces UpdateFactorMatrices (update.cuh:128-199): modes 0..N-1 in order */
 int gtk_update_factor_matrices(gtk_tensor *t);
 /* replaces Reconstruction (reconstruction.cuh:228-277): fit = 1 - sqrt(sum (x - x_hat)^2) / ||X||,
- * with the error summed in FP64 */
+ * with the error summed in FP64.  Right after an update of the last mode the error
+ * comes from that update: in the plain form from its stored delta, in the
+ * tensor-core forms from its Gram/RHS (err = ||X||^2 - sum_i (2 a_i.c_i -
+ * a_i^T G_i a_i), within ~1e-7 of the direct sum at fit 0.5); otherwise (factors
+ * or core set since) delta is recomputed per nonzero. */
 int gtk_reconstruction(gtk_tensor *t, double *fit);
 /* replaces the loop of TuckerDecomposition (tucker.cuh:166-187): up to max_iters sweeps
  * (each UpdateFactorMatrices then Reconstruction), stopping early when
@@ -208,7 +212,8 @@ int gtk_checkpoint_info(const char *path, int *order, int *rank, int *dtype, uin
  * form), GTK_VARIANT_REFERENCE_ORDER (delta of the update, the fit and
  * gtk_compute_delta in the reference's operation order, computing_delta_kernel,
  * delta.cuh:62-90: core entries in linear order, products left to right, each
- * rounded -- FP32 delta bit-identical to the reference's; slow, for parity).
+ * rounded -- FP32 delta bit-identical to the reference's; slow, for parity;
+ * selecting it first sums the reference's serial value_t norm on the host).
  * GTK_VARIANT_AUTO: tensor cores for the precision forms, SIMT2 otherwise.  gtk_set_kernel_variant forces one; gtk_autotune times the variants
  * that apply on the handle's mode-0 update (factor 0 restored afterwards), keeps
  * the fastest and caches it per (order, rank, value type, precision, log2 mean
