@@ -98,6 +98,7 @@ SIGNATURES = {
     "gtk_set_precision": (C.c_int, [P, C.c_int]),
     "gtk_update_mode": (C.c_int, [P, C.c_int]),
     "gtk_update_factor_matrices": (C.c_int, [P]),
+    "gtk_update_core": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
     "gtk_reconstruction": (C.c_int, [P, C.POINTER(C.c_double)]),
     "gtk_tucker_decomposition": (C.c_int, [P, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "gtk_compute_delta": (C.c_int, [P, C.c_int, P]),

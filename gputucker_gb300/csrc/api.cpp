@@ -103,7 +103,7 @@ static int put_factor(DevTensor &t, int n, const void *slabs) {
 
 static int get_factor(const DevTensor &t, int n, void *slabs) { return factor_to_host(t, n, slabs); }
 
-static int put_core(DevTensor &t, const void *core) {
+int put_core(DevTensor &t, const void *core) {
   fit_invalidate(t);
   GTK_CUDA(cudaMemcpyAsync(t.core, core, t.core_n * t.vsize, cudaMemcpyHostToDevice, t.stream));
   if (int rc = upload_core_perms(t, core)) return rc;
@@ -514,6 +514,14 @@ int gtk_update_mode(gtk_tensor *t, int mode) {
   if (mode < 0 || mode >= t->N) return fail(GTK_ERR_ARG, "mode out of range");
   GTK_GUARD_BEGIN
   return run_update_mode(*t, mode);
+  GTK_GUARD_END
+}
+
+int gtk_update_core(gtk_tensor *t, int cg_iters, int *iters_run, double *rel_residual) {
+  if (int rc = ready(t)) return rc;
+  if (cg_iters < 0) return fail(GTK_ERR_ARG, "negative iteration count");
+  GTK_GUARD_BEGIN
+  return run_update_core(*t, cg_iters, iters_run, rel_residual);
   GTK_GUARD_END
 }
 

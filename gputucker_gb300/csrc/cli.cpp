@@ -10,7 +10,9 @@
 // uses double), --device, --write-factors PREFIX (factor n in the slab layout,
 // one text row per factor row), --checkpoint PATH (factors, core and fits saved
 // after every sweep), --resume PATH (start from a saved checkpoint: its factors
-// and core, sweep count and last fit).  Without -p the partition comes from the
+// and core, sweep count and last fit), --core-update K (after each sweep's factor
+// updates, K conjugate-gradient steps of the least-squares core; the reference
+// never updates the core, so this changes results).  Without -p the partition comes from the
 // planner (gtk_plan_partition) with the device's free memory, as the
 // reference's TuckerDecomposition does (tucker.cuh:49-55).
 
@@ -41,7 +43,9 @@ static void usage() {
       "  --device arg (=0)      CUDA device\n"
       "  --write-factors PREFIX Write PREFIX<n>.txt per factor\n"
       "  --checkpoint PATH      Save factors, core and fits after every sweep\n"
-      "  --resume PATH          Continue from a checkpoint\n");
+      "  --resume PATH          Continue from a checkpoint\n"
+      "  --core-update K (=0)   K CG steps of the least-squares core after each sweep's\n"
+      "                         factor updates (not in the reference: changes results)\n");
 }
 
 static double now() {
@@ -59,7 +63,7 @@ static double now() {
 
 int main(int argc, char **argv) {
   std::string input, prefix, parts, ckpt, resume;
-  int order = -1, rank = 10, gpus = 1, iters = 3, dtype = GTK_F64, device = 0;
+  int order = -1, rank = 10, gpus = 1, iters = 3, dtype = GTK_F64, device = 0, core_update = 0;
   double tol = 1e-4;
   unsigned seed = 1;
   for (int i = 1; i < argc; ++i) {
@@ -106,6 +110,8 @@ int main(int argc, char **argv) {
       ckpt = val("checkpoint");
     } else if (a == "--resume") {
       resume = val("resume");
+    } else if (a == "--core-update") {
+      core_update = atoi(val("core-update"));
     } else {
       fprintf(stderr, "[ERROR] Parsing error : unrecognised option '%s'\n", a.c_str());
       usage();
@@ -201,6 +207,13 @@ int main(int argc, char **argv) {
     CHECK(gtk_update_factor_matrices(t));
     CHECK(gtk_synchronize(t));
     printf("Factor Time : %lf\n", now() - step);
+    if (core_update > 0) {
+      step = now();
+      int steps = 0;
+      double res = 0;
+      CHECK(gtk_update_core(t, core_update, &steps, &res));
+      printf("Core Time : %lf (%d CG steps, relative residual %.3g)\n", now() - step, steps, res);
+    }
     step = now();
     CHECK(gtk_reconstruction(t, &fit));
     printf("Recon Time : %lf\n\n", now() - step);

@@ -242,6 +242,15 @@ class BlockedTensor:
     def update_factor_matrices(self) -> None:
         call("gtk_update_factor_matrices", self.handle)
 
+    def update_core(self, cg_iters: int = 10) -> tuple[int, float]:
+        """Least-squares core with the factors fixed (no reference counterpart:
+        GPUTucker never updates G).  Returns (CG steps taken, relative residual
+        of the normal equations)."""
+        k = C.c_int()
+        res = C.c_double()
+        call("gtk_update_core", self.handle, cg_iters, C.byref(k), C.byref(res))
+        return k.value, res.value
+
     def reconstruction(self) -> float:
         f = C.c_double()
         call("gtk_reconstruction", self.handle, C.byref(f))

@@ -140,6 +140,16 @@ int gtk_set_precision(gtk_tensor *t, int precision);
 /* one mode update: delta, Gram/RHS (B = lambda*I + sum delta delta^T, C = sum x*delta)
  * and the J x J row solves a = C^T B^-1, all on the GPU (update.cuh:128-199 for one mode) */
 int gtk_update_mode(gtk_tensor *t, int mode);
+/* No reference counterpart (GPUTucker never updates the core; off unless called,
+ * and it changes results).  With the factors fixed, G minimises
+ * sum_t (x_t - <G, a_0[i_0] (x) ... (x) a_{N-1}[i_{N-1}]>)^2 + lambda ||G||^2
+ * (lambda = (double)0.0001f): up to cg_iters conjugate-gradient steps on its normal
+ * equations from the current core, each one pass of the plain delta kernels and
+ * one accumulation of sum_t y_t phi_t over the nonzeros.  At most 65536 core
+ * entries (rank^order).  *iters_run receives the steps taken (they stop early at
+ * a relative residual of 1e-14) and *rel_residual |b - H g| / |b| of the normal
+ * equations (either may be NULL).  On an error the core is put back. */
+int gtk_update_core(gtk_tensor *t, int cg_iters, int *iters_run, double *rel_residual);
 /* replaces UpdateFactorMatrices (update.cuh:128-199): modes 0..N-1 in order */
 int gtk_update_factor_matrices(gtk_tensor *t);
 /* replaces Reconstruction (reconstruction.cuh:228-277): fit = 1 - sqrt(sum (x - x_hat)^2) / ||X||,
