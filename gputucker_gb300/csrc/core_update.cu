@@ -13,7 +13,7 @@
 //     0..N1-1 and a right group N1..N-1, phi_t = l_t (x) r_t, so the sum is the
 //     outer product accumulation sum_t (y_t l_t) r_t^T of a (J^N1) x (J^(N-N1))
 //     matrix.  Per CTA a tile of nonzeros' l and r rows is built in shared memory;
-//     each thread owns a 4 x 4 block of the output, accumulates in value_t over
+//     each thread owns an 8 x 8 block of the output, accumulates in value_t over
 //     kFlushEvery nonzeros, then adds into FP64 with atomics.
 // The CG vectors (J^N <= 65536 entries) stay on the host in FP64.
 
@@ -30,6 +30,7 @@ namespace gtk {
 namespace {
 
 constexpr int kGradThreads = 256;
+constexpr int kBlk = 8;  // output block per thread: kBlk x kBlk
 constexpr int kFlushEvery = 1024;  // nonzeros per value_t partial sum before the FP64 flush
 constexpr uint64_t kCoreUpdateMaxCore = 65536;
 
@@ -75,16 +76,16 @@ __global__ void k_core_y(const V *__restrict__ delta, ModePtrs m, const uint64_t
 
 // out[l * SR + r] += sum_t w_t l_t[l] r_t[r] over the nonzeros [t_begin, t_end) of
 // this CTA's range; blockIdx.x = range * nchunks + chunk, chunk = which 256 of the
-// (SLp/4) x (SRp/4) output blocks this CTA's threads own
+// (SLp/8) x (SRp/8) output blocks of kBlk x kBlk this CTA's threads own
 template <class V>
 __global__ void __launch_bounds__(kGradThreads) k_core_grad(const V *__restrict__ w, ModePtrs m,
                                                             const uint64_t *__restrict__ blk_ptr, uint32_t nblk, int N,
                                                             int J, int ldf, uint64_t nnz, int N1, int SL, int SR,
                                                             int nbl, int nbr, int nchunks, uint64_t per,
                                                             double *__restrict__ out) {
-  constexpr int TN = sizeof(V) == 4 ? 16 : 8;  // nonzeros per tile
+  constexpr int TN = sizeof(V) == 4 ? 32 : 16;  // nonzeros per tile
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int SLp = nbl * 4, SRp = nbr * 4;
+  const int SLp = nbl * kBlk, SRp = nbr * kBlk;
   V *PL = reinterpret_cast<V *>(smem_raw);      // [TN][SLp]
   V *PR = PL + (size_t)TN * SLp;                // [TN][SRp]
   uint32_t *rows = reinterpret_cast<uint32_t *>(PR + (size_t)TN * SRp);  // [TN][N]
@@ -95,18 +96,18 @@ __global__ void __launch_bounds__(kGradThreads) k_core_grad(const V *__restrict_
   const uint64_t t_begin = range * per, t_end = min(nnz, t_begin + per);
   const int bi = chunk * kGradThreads + tid;  // this thread's output block
   const bool active = bi < nbl * nbr;
-  const int l0 = active ? (bi / nbr) * 4 : 0, r0 = active ? (bi % nbr) * 4 : 0;
-  V acc[4][4];
+  const int l0 = active ? (bi / nbr) * kBlk : 0, r0 = active ? (bi % nbr) * kBlk : 0;
+  V acc[kBlk][kBlk];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < kBlk; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = V(0);
+    for (int j = 0; j < kBlk; ++j) acc[i][j] = V(0);
   auto flush = [&]() {
     if (!active) return;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < kBlk; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < kBlk; ++j) {
         if (l0 + i < SL && r0 + j < SR && acc[i][j] != V(0))
           atomicAdd(out + (size_t)(l0 + i) * SR + (r0 + j), (double)acc[i][j]);
         acc[i][j] = V(0);
@@ -160,15 +161,15 @@ __global__ void __launch_bounds__(kGradThreads) k_core_grad(const V *__restrict_
     __syncthreads();
     if (active) {
       for (int tt = 0; tt < nt; ++tt) {
-        V lv[4], rv[4];
+        V lv[kBlk], rv[kBlk];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) lv[i] = PL[tt * SLp + l0 + i];
+        for (int i = 0; i < kBlk; ++i) lv[i] = PL[tt * SLp + l0 + i];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) rv[j] = PR[tt * SRp + r0 + j];
+        for (int j = 0; j < kBlk; ++j) rv[j] = PR[tt * SRp + r0 + j];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < kBlk; ++i)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] += lv[i] * rv[j];
+          for (int j = 0; j < kBlk; ++j) acc[i][j] += lv[i] * rv[j];
       }
     }
     since_flush += nt;
@@ -209,10 +210,11 @@ template <class V> int update_core_impl(DevTensor &t, int iters, int *iters_run,
   int SL = 1, SR = 1;
   for (int k = 0; k < N1; ++k) SL *= J;
   for (int k = N1; k < N; ++k) SR *= J;
-  const int nbl = (SL + 3) / 4, nbr = (SR + 3) / 4;
+  const int nbl = (SL + kBlk - 1) / kBlk, nbr = (SR + kBlk - 1) / kBlk;
   const int nchunks = (nbl * nbr + kGradThreads - 1) / kGradThreads;
-  constexpr int TN = sizeof(V) == 4 ? 16 : 8;
-  const size_t smem = ((size_t)TN * (nbl + nbr) * 4 * sizeof(V) + TN * kMaxOrder * 4 + 16 + TN * sizeof(V) + 15) / 16 * 16;
+  constexpr int TN = sizeof(V) == 4 ? 32 : 16;
+  const size_t smem =
+      ((size_t)TN * (nbl + nbr) * kBlk * sizeof(V) + TN * kMaxOrder * 4 + 16 + TN * sizeof(V) + 15) / 16 * 16;
   if (smem > 200 * 1024) return fail(GTK_ERR_UNSUPPORTED, "core update: the core's factor groups are too wide");
   GTK_CUDA(cudaFuncSetAttribute((const void *)k_core_grad<V>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const uint64_t target = (uint64_t)t.num_sms * 4;
