@@ -278,6 +278,10 @@ def run_precision3d(args, dist):
 
     import gputucker_gb300 as gtk
     cfg = dict(PREC3D)
+    if args.shape:  # ORDER,RANK,DIM[,P]: a smaller instance with the configuration's row lengths (profiling)
+        f = [int(x) for x in args.shape.split(",")]
+        cfg.update(workload=f"precision{f[0]}d_{f[2]}_rank{f[1]}", order=f[0], dims=[f[2]] * f[0], rank=f[1],
+                   partition=[f[3] if len(f) > 3 else 1] * f[0])
     nnz = args.nnz or cfg["nnz"]
     S = cfg["compare_sweeps"]
     t0 = time.perf_counter()
