@@ -24,7 +24,8 @@ fit after the K sweeps is within 1e-4 of the plain form's, else the plain form's
   e2e .......... the whole job through the C ABI with host buffers: upload the
                  pinned host COO, partition and segment it on the GPU, initialise,
                  run the configuration's 10 sweeps with a fit each, read the
-                 factors back -- N * nnz * sweeps / wall time.
+                 factors back -- N * nnz * sweeps / wall time of the fastest of
+                 --e2e-runs (default 3) jobs; every job's wall time is listed.
   roofline ..... the dominant kernel (fused delta + Gram/RHS) of the chosen form:
                  the compulsory bytes of the unfused delta (4N + 4J per nonzero and mode)
                  per launch over its event-timed duration, against the measured
@@ -32,6 +33,11 @@ fit after the K sweeps is within 1e-4 of the plain form's, else the plain form's
   cpu_baseline . the CPU restatement of the reference (its OpenMP delta/B,C/LU
                  path, oracle/gtk_oracle.cpp) on a bounded sample of the same
                  tensor, all host threads.
+
+Other workloads (--workload): batch256 (256 independent tensors, one graph launch
+per sweep), warmstart (the learned warm start on the planted 50,000^3 family),
+precision3d (the 3-order 500M-nonzero rank-16 tensor: plain FP32, BF16 and TF32
+timed like the headline and compared after 3 sweeps with an FP64 run).
 
 --impl reference times that CPU path alone (the reference's own code is CPU +
 an sm_70 SIMT kernel with no Blackwell build; the restatement is its path).
