@@ -12,7 +12,9 @@
 // after every sweep), --resume PATH (start from a saved checkpoint: its factors
 // and core, sweep count and last fit), --core-update K (after each sweep's factor
 // updates, K conjugate-gradient steps of the least-squares core; the reference
-// never updates the core, so this changes results).  Without -p the partition comes from the
+// never updates the core, so this changes results), --precision plain|bf16|tf32
+// (the tensor-core form of the delta contraction and Gram/RHS, FP32 values only;
+// default plain, the reference's arithmetic).  Without -p the partition comes from the
 // planner (gtk_plan_partition) with the device's free memory, as the
 // reference's TuckerDecomposition does (tucker.cuh:49-55).
 
@@ -44,6 +46,7 @@ static void usage() {
       "  --write-factors PREFIX Write PREFIX<n>.txt per factor\n"
       "  --checkpoint PATH      Save factors, core and fits after every sweep\n"
       "  --resume PATH          Continue from a checkpoint\n"
+      "  --precision plain|bf16|tf32 (=plain)  Tensor-core form (needs --dtype f32)\n"
       "  --core-update K (=0)   K CG steps of the least-squares core after each sweep's\n"
       "                         factor updates (not in the reference: changes results)\n");
 }
@@ -63,7 +66,8 @@ static double now() {
 
 int main(int argc, char **argv) {
   std::string input, prefix, parts, ckpt, resume;
-  int order = -1, rank = 10, gpus = 1, iters = 3, dtype = GTK_F64, device = 0, core_update = 0;
+  int order = -1, rank = 10, gpus = 1, iters = 3, dtype = GTK_F64, device = 0, core_update = 0,
+      precision = GTK_PREC_PLAIN;
   double tol = 1e-4;
   unsigned seed = 1;
   for (int i = 1; i < argc; ++i) {
@@ -112,6 +116,15 @@ int main(int argc, char **argv) {
       resume = val("resume");
     } else if (a == "--core-update") {
       core_update = atoi(val("core-update"));
+    } else if (a == "--precision") {
+      const std::string pr = val("precision");
+      if (pr == "plain") precision = GTK_PREC_PLAIN;
+      else if (pr == "bf16") precision = GTK_PREC_BF16;
+      else if (pr == "tf32") precision = GTK_PREC_TF32;
+      else {
+        fprintf(stderr, "[ERROR] --precision must be plain, bf16 or tf32\n");
+        return 2;
+      }
     } else {
       fprintf(stderr, "[ERROR] Parsing error : unrecognised option '%s'\n", a.c_str());
       usage();
@@ -187,6 +200,7 @@ int main(int argc, char **argv) {
   for (int n = 0; n < order; ++n) printf("Partition dim[%d] = %u\tBlock dim[%d] = %u\n", n, P[n], n, info.block_dims[n]);
   printf("# blocks: %llu\n", (unsigned long long)info.block_count);
   CHECK(gtk_init_random(t, seed, draws));
+  if (precision != GTK_PREC_PLAIN) CHECK(gtk_set_precision(t, precision));
   double p_fit = -1, fit = -1;
   int it = 0;
   std::vector<double> fits;

@@ -138,3 +138,34 @@ def test_streamed_tensor_core_form(case):
         tb.set_graph(True)
         tg_fit = [tb.sweep() for _ in range(2)]
         assert all(np.isfinite(tg_fit))
+
+
+def test_cli_precision_form(tmp_path):
+    """--precision bf16 on the CLI runs the tensor-core form: the fits equal the
+    same sweeps through the Python mirror (up to the order of FP64 atomic adds)."""
+    import re
+    import subprocess
+
+    from gputucker_gb300 import build
+    from oracle_util import random_coo, write_tns
+    rng = np.random.default_rng(21)
+    dims = [30, 35, 40, 45]
+    idx = random_coo(rng, dims, 20000)
+    vals = rng.random(len(idx[0]))
+    f = tmp_path / "t.tns"
+    write_tns(f, idx, vals, dtype=0)
+    r = subprocess.run([build.CLI, "-i", str(f), "-o", "4", "-r", "10", "-p", "2,1,1,2", "--dtype", "f32",
+                        "--precision", "bf16", "--iters", "3", "--tol", "0"], capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    fits = [float(x) for x in re.findall(r"^iter \d+\t Fit: (\S+)$", r.stdout, flags=re.M)]
+    coo = gtk.parse_from_file(str(f), 4, "f32", rand_seed=1)
+    with gtk.create_tensor_blocks(coo, [2, 1, 1, 2], 10) as t:
+        t.init_random(1, coo.rand_draws)
+        t.set_precision("bf16")
+        ref = []
+        for _ in range(3):
+            t.update_factor_matrices()
+            ref.append(t.reconstruction())
+    print(fits, ref)
+    np.testing.assert_allclose(fits, ref, rtol=0, atol=1e-6)
