@@ -87,6 +87,34 @@ def build(verbose: bool = False, ptxas_verbose: bool = False) -> str:
     return LIB
 
 
+SANITIZE = ["-fsanitize=address", "-fsanitize=undefined", "-fno-omit-frame-pointer", "-fno-sanitize-recover=undefined"]
+
+
+def build_host_sanitized(out_dir: str) -> str:
+    """The library with its host-only C++ sources (parser, generator, planner and
+    checkpoint, API layer) compiled under AddressSanitizer + UndefinedBehavior-
+    Sanitizer, linked with the regular objects of the CUDA sources, into
+    out_dir/libgputucker_gb300.so (for the host sanitizer test; a program that
+    loads it must be built with the same -fsanitize flags)."""
+    build()
+    os.makedirs(out_dir, exist_ok=True)
+    nvcc = _nvcc()
+    jobs, objs = [], []
+    for src in LIB_SOURCES:
+        if src.endswith(".cpp"):
+            obj = os.path.join(out_dir, src + ".o")
+            jobs.append([nvcc, "-c", os.path.join(CSRC, src), "-o", obj, "-O1", "-g", "-std=c++17", "-Xcompiler",
+                         "-fPIC,-ffp-contract=off," + ",".join(SANITIZE), "-I" + INCLUDE, "-I" + CSRC] + ARCH)
+            objs.append(obj)
+        else:
+            objs.append(os.path.join(BUILD, src + ".o"))
+    with ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 1))) as ex:
+        list(ex.map(_run_logged(False), jobs))
+    lib = os.path.join(out_dir, "libgputucker_gb300.so")
+    _run([nvcc, "-shared", "-o", lib] + objs + ARCH + ["-lpthread", "-Xcompiler", ",".join(SANITIZE)])
+    return lib
+
+
 def _run_logged(verbose: bool):
     def f(cmd: list[str]) -> None:
         if verbose:

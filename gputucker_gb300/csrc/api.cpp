@@ -254,6 +254,7 @@ void gtk_coo_free(gtk_coo *c) {
 }
 
 int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int device, gtk_tensor **out) {
+  NvtxRange nvtx("gtk_create_blocks");
   if (!coo || !P || !out) return fail(GTK_ERR_ARG, "null argument");
   if (rank < 1 || rank > GTK_MAX_RANK) return fail(GTK_ERR_ARG, "rank must be 1..64");
   const int N = coo->N;

@@ -291,6 +291,7 @@ int gtk_batch_create(gtk_tensor *const *tensors, int count, gtk_batch **out) {
 }
 
 int gtk_batch_sweep(gtk_batch *b, double *fits) {
+  NvtxRange nvtx("gtk_batch_sweep");
   if (!b) return fail(GTK_ERR_ARG, "null batch");
   GTK_CUDA(cudaSetDevice(b->dev));
   for (gtk_tensor *t : b->ts)

@@ -310,6 +310,7 @@ template <class V> int update_core_impl(DevTensor &t, int iters, int *iters_run,
 }  // namespace
 
 int run_update_core(DevTensor &t, int iters, int *iters_run, double *rel_residual) {
+  NvtxRange nvtx("gtk_update_core");
   if (t.core_n > kCoreUpdateMaxCore)
     return fail(GTK_ERR_UNSUPPORTED, "core update: at most 65536 core entries (rank^order)");
   if (!t.nnz) return fail(GTK_ERR_STATE, "core update of an empty tensor");

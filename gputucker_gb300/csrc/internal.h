@@ -2,12 +2,22 @@
 #pragma once
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
 #include <string>
 #include <vector>
 
 #include "gputucker_gb300.h"
+
+// NVTX range around a host-side stage (create, mode update, fit, sweep, batch
+// sweep, warm-start training, core update): a no-op unless a profiler is attached
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
 
 namespace gtk {
 

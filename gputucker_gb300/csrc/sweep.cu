@@ -1103,6 +1103,9 @@ void fit_after_sweep(DevTensor &t) {
 }
 
 template <class V> static int update_impl(DevTensor &t, int mode) {
+  static const char *const kNames[kMaxOrder] = {"mode update 0", "mode update 1", "mode update 2", "mode update 3",
+                                                 "mode update 4", "mode update 5", "mode update 6", "mode update 7"};
+  NvtxRange nvtx(kNames[mode]);
   const int E = pairs_for(t.J);
   const int J = t.J;
   const bool last = mode == t.N - 1;
@@ -1205,6 +1208,7 @@ int run_update_mode(DevTensor &t, int mode) {
 
 // the fit kernels: the error of every nonzero summed into t.partial[kFitGridMax]
 template <class V> static int fit_enqueue(DevTensor &t) {
+  NvtxRange nvtx("fit");
   int grid = 1;
   if (t.variant == kVarRefOrder && t.nnz) {
     // x_hat into the delta store's memory (nnz values), then the serial error
@@ -1295,6 +1299,7 @@ void drop_graph(DevTensor &t) {
 // kernels -- is captured once into a CUDA graph and replayed; only the 8-byte
 // read of the error sum stays outside.
 int run_sweep(DevTensor &t, double *fit) {
+  NvtxRange nvtx("sweep");
   if (!t.use_graph) {
     for (int n = 0; n < t.N; ++n)
       if (int rc = run_update_mode(t, n)) return rc;

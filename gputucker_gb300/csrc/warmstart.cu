@@ -691,6 +691,7 @@ int gtk_ws_predict(gtk_ws *m, const float *x, int B, float *y) {
 }
 
 int gtk_ws_train(gtk_ws *m, int steps, int batch, float lr, double *final_loss) {
+  NvtxRange nvtx("gtk_ws_train");
   if (!m || steps < 0 || batch < 1) return fail(GTK_ERR_ARG, "bad argument");
   if (!m->ex_n) return fail(GTK_ERR_STATE, "no training examples (gtk_ws_add_example)");
   GTK_CUDA(cudaSetDevice(m->dev));
