@@ -121,6 +121,8 @@ SIGNATURES = {
     "gtk_ws_create": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_uint64, C.c_int, C.POINTER(P)]),
     "gtk_ws_destroy": (None, [P]),
     "gtk_ws_info": (C.c_int, [P, C.POINTER(C.c_int), U64P, U64P]),
+    "gtk_ws_save": (C.c_int, [P, C.c_char_p]),
+    "gtk_ws_load": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(P)]),
     "gtk_ws_get_params": (C.c_int, [P, P, P, P]),
     "gtk_ws_set_params": (C.c_int, [P, P, P, P]),
     "gtk_ws_features": (C.c_int, [P, C.c_int, P]),

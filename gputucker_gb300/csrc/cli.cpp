@@ -14,7 +14,9 @@
 // updates, K conjugate-gradient steps of the least-squares core; the reference
 // never updates the core, so this changes results), --precision plain|bf16|tf32
 // (the tensor-core form of the delta contraction and Gram/RHS, FP32 values only;
-// default plain, the reference's arithmetic).  Without -p the partition comes from the
+// default plain, the reference's arithmetic), --init-model PATH (a learned warm
+// start saved by gtk_ws_save: its predicted factor rows replace the random ones,
+// the core stays the random draw).  Without -p the partition comes from the
 // planner (gtk_plan_partition) with the device's free memory, as the
 // reference's TuckerDecomposition does (tucker.cuh:49-55).
 
@@ -47,6 +49,7 @@ static void usage() {
       "  --checkpoint PATH      Save factors, core and fits after every sweep\n"
       "  --resume PATH          Continue from a checkpoint\n"
       "  --precision plain|bf16|tf32 (=plain)  Tensor-core form (needs --dtype f32)\n"
+      "  --init-model PATH      Initial factors from a saved warm-start model\n"
       "  --core-update K (=0)   K CG steps of the least-squares core after each sweep's\n"
       "                         factor updates (not in the reference: changes results)\n");
 }
@@ -65,7 +68,7 @@ static double now() {
   } while (0)
 
 int main(int argc, char **argv) {
-  std::string input, prefix, parts, ckpt, resume;
+  std::string input, prefix, parts, ckpt, resume, init_model;
   int order = -1, rank = 10, gpus = 1, iters = 3, dtype = GTK_F64, device = 0, core_update = 0,
       precision = GTK_PREC_PLAIN;
   double tol = 1e-4;
@@ -116,6 +119,8 @@ int main(int argc, char **argv) {
       resume = val("resume");
     } else if (a == "--core-update") {
       core_update = atoi(val("core-update"));
+    } else if (a == "--init-model") {
+      init_model = val("init-model");
     } else if (a == "--precision") {
       const std::string pr = val("precision");
       if (pr == "plain") precision = GTK_PREC_PLAIN;
@@ -200,6 +205,14 @@ int main(int argc, char **argv) {
   for (int n = 0; n < order; ++n) printf("Partition dim[%d] = %u\tBlock dim[%d] = %u\n", n, P[n], n, info.block_dims[n]);
   printf("# blocks: %llu\n", (unsigned long long)info.block_count);
   CHECK(gtk_init_random(t, seed, draws));
+  if (!init_model.empty()) {
+    gtk_ws *m = nullptr;
+    CHECK(gtk_ws_load(init_model.c_str(), device, &m));
+    const int rc = gtk_ws_apply(m, t);
+    gtk_ws_destroy(m);
+    CHECK(rc);
+    printf("Initial factors from %s\n", init_model.c_str());
+  }
   if (precision != GTK_PREC_PLAIN) CHECK(gtk_set_precision(t, precision));
   double p_fit = -1, fit = -1;
   int it = 0;

@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -556,6 +557,80 @@ void gtk_ws_destroy(gtk_ws *m) {
   if (m->loss) cudaFree(m->loss);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
+}
+
+// model file: "GTKWS001", u32 order, rank, hidden, features, u64 params, then the
+// params, the feature means and standard deviations (float), then the FNV-1a 64
+// checksum of everything before it
+static const char kWsMagic[8] = {'G', 'T', 'K', 'W', 'S', '0', '0', '1'};
+static uint64_t fnv1a(const unsigned char *p, size_t n, uint64_t h) {
+  for (size_t i = 0; i < n; ++i) h = (h ^ p[i]) * 1099511628211ull;
+  return h;
+}
+
+int gtk_ws_save(const gtk_ws *m, const char *path) {
+  if (!m || !path) return fail(GTK_ERR_ARG, "null argument");
+  if (!m->have_norm) return fail(GTK_ERR_STATE, "the model is untrained");
+  std::vector<unsigned char> buf;
+  auto put = [&](const void *p, size_t n) {
+    const unsigned char *c = static_cast<const unsigned char *>(p);
+    buf.insert(buf.end(), c, c + n);
+  };
+  const uint32_t hdr[4] = {(uint32_t)m->N, (uint32_t)m->J, (uint32_t)m->H, (uint32_t)m->F};
+  const uint64_t np = m->np;
+  put(kWsMagic, 8);
+  put(hdr, sizeof(hdr));
+  put(&np, 8);
+  std::vector<float> w(m->np);
+  GTK_CUDA(cudaSetDevice(m->dev));
+  GTK_CUDA(cudaMemcpy(w.data(), m->w, m->np * 4, cudaMemcpyDeviceToHost));
+  put(w.data(), w.size() * 4);
+  put(m->fmean.data(), (size_t)m->F * 4);
+  put(m->fstd.data(), (size_t)m->F * 4);
+  const uint64_t h = fnv1a(buf.data(), buf.size(), 1469598103934665603ull);
+  put(&h, 8);
+  const std::string tmp = std::string(path) + ".tmp";
+  FILE *f = fopen(tmp.c_str(), "wb");
+  if (!f) return fail(GTK_ERR_IO, "cannot write " + tmp);
+  const bool ok = fwrite(buf.data(), 1, buf.size(), f) == buf.size();
+  if (fclose(f) != 0 || !ok || rename(tmp.c_str(), path) != 0) return fail(GTK_ERR_IO, "cannot write " + std::string(path));
+  return 0;
+}
+
+int gtk_ws_load(const char *path, int device, gtk_ws **out) {
+  if (!path || !out) return fail(GTK_ERR_ARG, "null argument");
+  FILE *f = fopen(path, "rb");
+  if (!f) return fail(GTK_ERR_IO, "cannot open " + std::string(path));
+  std::vector<unsigned char> buf;
+  unsigned char chunk[1 << 16];
+  size_t n;
+  while ((n = fread(chunk, 1, sizeof(chunk), f)) > 0) buf.insert(buf.end(), chunk, chunk + n);
+  fclose(f);
+  const size_t head = 8 + 16 + 8;
+  if (buf.size() < head + 8 || memcmp(buf.data(), kWsMagic, 8) != 0) return fail(GTK_ERR_PARSE, "not a warm-start model");
+  uint32_t hdr[4];
+  uint64_t np = 0, h = 0;
+  memcpy(hdr, buf.data() + 8, 16);
+  memcpy(&np, buf.data() + 24, 8);
+  const uint64_t F = hdr[3];
+  if (hdr[0] < 2 || hdr[0] > kMaxOrder || hdr[1] < 1 || hdr[1] > kMaxRank || hdr[2] < 1 || hdr[2] > 1024 ||
+      np > (1ull << 32) || F > 1024 || buf.size() != head + np * 4 + 2 * F * 4 + 8)
+    return fail(GTK_ERR_PARSE, "damaged warm-start model");
+  memcpy(&h, buf.data() + buf.size() - 8, 8);
+  if (fnv1a(buf.data(), buf.size() - 8, 1469598103934665603ull) != h) return fail(GTK_ERR_PARSE, "checksum mismatch");
+  gtk_ws *m = nullptr;
+  if (int rc = gtk_ws_create((int)hdr[0], (int)hdr[1], (int)hdr[2], 0, device, &m)) return rc;
+  if (m->np != np || (uint64_t)m->F != F) {
+    gtk_ws_destroy(m);
+    return fail(GTK_ERR_PARSE, "model layout does not match its order, rank and width");
+  }
+  const float *p = reinterpret_cast<const float *>(buf.data() + head);
+  if (int rc = gtk_ws_set_params(m, p, p + np, p + np + F)) {
+    gtk_ws_destroy(m);
+    return rc;
+  }
+  *out = m;
+  return 0;
 }
 
 int gtk_ws_info(const gtk_ws *m, int *features, uint64_t *params, uint64_t *examples) {

@@ -457,6 +457,24 @@ class WarmStart:
     def apply(self, t: BlockedTensor) -> None:
         call("gtk_ws_apply", self.handle, t.handle)
 
+    def save(self, path: str) -> None:
+        """The trained model to a file (gtk_ws_save)."""
+        call("gtk_ws_save", self.handle, str(path).encode())
+
+    @classmethod
+    def load(cls, path: str, device: int = 0) -> "WarmStart":
+        """A model saved by save() (gtk_ws_load)."""
+        h = C.c_void_p()
+        call("gtk_ws_load", str(path).encode(), device, C.byref(h))
+        m = cls.__new__(cls)
+        m._h = h
+        f, n = C.c_int(), C.c_uint64()
+        call("gtk_ws_info", h, C.byref(f), C.byref(n), None)
+        m.features, m.n_params = f.value, n.value
+        with open(path, "rb") as fh:  # order, rank, width from the header (checked by gtk_ws_load)
+            m.order, m.rank, m.hidden, _ = np.frombuffer(fh.read(24)[8:], np.uint32).tolist()
+        return m
+
     def get_params(self):
         p = np.empty(self.n_params, np.float32)
         mu = np.empty(self.features, np.float32)

@@ -277,6 +277,11 @@ typedef struct gtk_ws gtk_ws;
 int gtk_ws_create(int order, int rank, int hidden, uint64_t seed, int device, gtk_ws **out);
 void gtk_ws_destroy(gtk_ws *m);
 int gtk_ws_info(const gtk_ws *m, int *features, uint64_t *params, uint64_t *examples);
+/* a trained model to / from a file (order, rank, width, weights, feature
+ * standardisation; FNV-1a checksum; written to path.tmp then renamed).
+ * gtk_ws_load creates the model on `device`; a damaged file is GTK_ERR_PARSE. */
+int gtk_ws_save(const gtk_ws *m, const char *path);
+int gtk_ws_load(const char *path, int device, gtk_ws **out);
 int gtk_ws_get_params(const gtk_ws *m, float *params, float *feat_mean, float *feat_std);
 int gtk_ws_set_params(gtk_ws *m, const float *params, const float *feat_mean, const float *feat_std);
 int gtk_ws_features(gtk_tensor *t, int mode, float *out);  /* raw features, rows of mode x F, host */

@@ -3,7 +3,7 @@
 // and this driver with -fsanitize=address,undefined; no GPU is touched).
 // Exercises the parser on well-formed and malformed text, the generator, the text
 // writer (round trip through the parser), the partition planner and the
-// checkpoint header reader on damaged files.  Exit status 0 when every call
+// checkpoint and warm-start model readers on damaged files.  Exit status 0 when every call
 // returned what it should; the sanitizers abort on any memory or UB error.
 
 #include <cstdio>
@@ -110,6 +110,22 @@ int main(int argc, char **argv) {
       if (len) fwrite(junk.data(), 1, len, f);
       fclose(f);
       EXPECT(gtk_checkpoint_info(bad.c_str(), &order, &rank, &dtype, dims, parts, &nfits) != 0);
+    }
+  }
+  // warm-start model reader on missing, truncated and garbage files (rejected
+  // before any device is touched)
+  {
+    gtk_ws *m = nullptr;
+    EXPECT(gtk_ws_load((dir + "/none.ws").c_str(), 0, &m) == GTK_ERR_IO);
+    const std::string bad = dir + "/bad.ws";
+    for (size_t len : {0, 7, 8, 32, 40, 400}) {
+      FILE *f = fopen(bad.c_str(), "wb");
+      std::vector<unsigned char> junk(len);
+      for (size_t k = 0; k < len; ++k) junk[k] = (unsigned char)(k * 37 + 11);
+      if (len >= 8) memcpy(junk.data(), "GTKWS001", 8);
+      if (len) fwrite(junk.data(), 1, len, f);
+      fclose(f);
+      EXPECT(gtk_ws_load(bad.c_str(), 0, &m) == GTK_ERR_PARSE);
     }
   }
   if (failures) fprintf(stderr, "%d expectation(s) failed\n", failures);

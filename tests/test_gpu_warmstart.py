@@ -110,3 +110,49 @@ def test_warm_start_gains_over_random_init():
             gains.append((K, n_warm, plain[0], warm[0]))
             assert warm[0] > plain[0], (plain, warm)
         assert sum(g[1] for g in gains) <= sum(g[0] for g in gains) / 2, gains
+
+
+def test_model_save_load_and_cli_init(tmp_path):
+    """A trained model saved and loaded predicts the same rows; the CLI's
+    --init-model starts from the same factors as WarmStart.apply (its fits equal
+    the Python path's)."""
+    import re
+    import subprocess
+
+    from gputucker_gb300 import build
+    coo = gtk.generate_planted(3, [2000, 2100, 2200], 200_000, 4, 0.01, "f64", seed=5)
+    with gtk.create_tensor_blocks(coo, [1, 1, 1], 4) as t:
+        t.init_random(1, 0)
+        for _ in range(5):
+            t.sweep()
+        ws = gtk.WarmStart(3, 4, hidden=16, seed=2)
+        ws.add_example(t)
+        ws.train(200, 512, 1e-3)
+        path = tmp_path / "model.ws"
+        ws.save(path)
+        m = gtk.WarmStart.load(path)
+        assert (m.order, m.rank, m.hidden) == (3, 4, 16)
+        for a, b in zip(ws.get_params(), m.get_params()):
+            assert np.array_equal(a, b)
+        x = np.random.default_rng(0).random((64, ws.features)).astype(np.float32)
+        assert np.array_equal(ws.predict(x), m.predict(x))
+        f = tmp_path / "t.tns"
+        coo.write_text(f)
+        ws.close()
+        m.close()
+    m = gtk.WarmStart.load(path)
+    c2 = gtk.parse_from_file(str(f), 3, "f64", rand_seed=1)
+    with gtk.create_tensor_blocks(c2, [1, 1, 1], 4) as t:
+        t.init_random(1, c2.rand_draws)
+        m.apply(t)
+        ref = []
+        for _ in range(3):
+            t.update_factor_matrices()
+            ref.append(t.reconstruction())
+    m.close()
+    r = subprocess.run([build.CLI, "-i", str(f), "-o", "3", "-r", "4", "-p", "1,1,1", "--iters", "3", "--tol", "0",
+                        "--init-model", str(path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    fits = [float(x) for x in re.findall(r"^iter \d+\t Fit: (\S+)$", r.stdout, flags=re.M)]
+    print(fits, ref)
+    np.testing.assert_allclose(fits, ref, rtol=0, atol=1e-9)
