@@ -35,6 +35,7 @@ GTK_VAL_LOGNORMAL = 1
 GTK_VAL_PLANTED = 2
 GTK_MAX_ORDER = 8
 GTK_MAX_RANK = 64
+GTK_VALIDATE_CHECKS = 8
 
 STATUS_NAMES = {
     GTK_ERR_ARG: "GTK_ERR_ARG", GTK_ERR_IO: "GTK_ERR_IO", GTK_ERR_PARSE: "GTK_ERR_PARSE",
@@ -99,6 +100,7 @@ SIGNATURES = {
     "gtk_update_mode": (C.c_int, [P, C.c_int]),
     "gtk_update_factor_matrices": (C.c_int, [P]),
     "gtk_update_core": (C.c_int, [P, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_double)]),
+    "gtk_validate": (C.c_int, [P, U64P]),
     "gtk_reconstruction": (C.c_int, [P, C.POINTER(C.c_double)]),
     "gtk_tucker_decomposition": (C.c_int, [P, C.c_int, C.c_double, C.POINTER(C.c_double), C.POINTER(C.c_int)]),
     "gtk_compute_delta": (C.c_int, [P, C.c_int, P]),

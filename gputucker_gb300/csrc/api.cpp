@@ -518,6 +518,14 @@ int gtk_update_mode(gtk_tensor *t, int mode) {
   GTK_GUARD_END
 }
 
+int gtk_validate(gtk_tensor *t, uint64_t *violations) {
+  if (!t || !violations) return fail(GTK_ERR_ARG, "null argument");
+  if (int rc = set_dev(t)) return rc;
+  GTK_GUARD_BEGIN
+  return run_validate(*t, violations);
+  GTK_GUARD_END
+}
+
 int gtk_update_core(gtk_tensor *t, int cg_iters, int *iters_run, double *rel_residual) {
   if (int rc = ready(t)) return rc;
   if (cg_iters < 0) return fail(GTK_ERR_ARG, "negative iteration count");

@@ -193,6 +193,7 @@ int ensure_dstore(DevTensor &t);
 int ensure_norm_ref(DevTensor &t);  // the reference's value_t norm from val_in (host, serial)
 int put_core(DevTensor &t, const void *core_host);  // core in linear order -> core, corep, images
 int run_update_core(DevTensor &t, int cg_iters, int *iters_run, double *rel_residual);
+int run_validate(DevTensor &t, uint64_t *violations);  // GTK_VALIDATE_CHECKS counters
 int factor_to_host(const DevTensor &t, int n, void *slabs);    // device [rows][ldf] -> host [rows][J]
 int factor_from_host(DevTensor &t, int n, const void *slabs);  // host [rows][J] -> device [rows][ldf]
 void fit_invalidate(DevTensor &t);         // factors, core or kernel changed: the next fit recomputes

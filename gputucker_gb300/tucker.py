@@ -242,6 +242,13 @@ class BlockedTensor:
     def update_factor_matrices(self) -> None:
         call("gtk_update_factor_matrices", self.handle)
 
+    def validate(self) -> list[int]:
+        """gtk_validate: violation counts of the device arrays' consistency checks
+        (all zero for a handle built by create_tensor_blocks)."""
+        out = np.zeros(nat.GTK_VALIDATE_CHECKS, np.uint64)
+        call("gtk_validate", self.handle, out.ctypes.data_as(nat.U64P))
+        return [int(x) for x in out]
+
     def update_core(self, cg_iters: int = 10) -> tuple[int, float]:
         """Least-squares core with the factors fixed (no reference counterpart:
         GPUTucker never updates G).  Returns (CG steps taken, relative residual

@@ -150,6 +150,16 @@ int gtk_update_mode(gtk_tensor *t, int mode);
  * a relative residual of 1e-14) and *rel_residual |b - H g| / |b| of the normal
  * equations (either may be NULL).  On an error the core is put back. */
 int gtk_update_core(gtk_tensor *t, int cg_iters, int *iters_run, double *rel_residual);
+/* No reference counterpart.  Consistency checks of a handle's device arrays,
+ * one pass over each (no trap, no stop): violations[c] counts, for c =
+ *   0 block-local coordinates >= block_dims[n], 1 view coordinates >= dims[k],
+ *   2 view entries out of row order, 3 view permutation entries >= nnz,
+ *   4 where_nnz entries >= their block's size, 5 count_nnz row pointers that
+ *   decrease, do not start at 0 or do not end at the block's size, 6 non-finite
+ *   factor or core entries, 7 block pointers that decrease, do not end at nnz or
+ *   differ from the host copy.  All zero for a handle built by gtk_create_blocks. */
+#define GTK_VALIDATE_CHECKS 8
+int gtk_validate(gtk_tensor *t, uint64_t *violations);
 /* replaces UpdateFactorMatrices (update.cuh:128-199): modes 0..N-1 in order */
 int gtk_update_factor_matrices(gtk_tensor *t);
 /* replaces Reconstruction (reconstruction.cuh:228-277): fit = 1 - sqrt(sum (x - x_hat)^2) / ||X||,
