@@ -260,7 +260,7 @@ template <class V, int KE, bool EXACT> struct GramAcc {
   }
   // tile positions [t0, t1) of the shared delta tile (row stride ldd, column J = x)
   __device__ void run(const V *dx, int ldd, const uint32_t *rows, int t0, int t1, double *gram, int E, int lane) {
-    if (EXACT) {
+    if constexpr (EXACT) {
       for (int t = t0; t < t1; ++t) {
         const uint32_t r = rows[t];
         if (r != row) {
@@ -271,8 +271,7 @@ template <class V, int KE, bool EXACT> struct GramAcc {
 #pragma unroll
         for (int k = 0; k < KE; ++k) acc[k].add(mul_rn(d[ei[k]], d[ej[k]]));
       }
-      return;
-    }
+    } else {
     // runs of equal rows, 32 positions at a time: one ballot finds where rows change
     for (int base = t0; base < t1; base += 32) {
       const int n = min(32, t1 - base);
@@ -312,6 +311,7 @@ template <class V, int KE, bool EXACT> struct GramAcc {
         heads = b - a >= 32 ? 0u : (heads >> (b - a));
         a = b;
       }
+    }
     }
   }
 };

@@ -110,8 +110,7 @@ __device__ __forceinline__ void cp_async_wait1() { asm volatile("cp.async.wait_g
 // input of one Nest<3>.  Two chunk buffers; chunk c+1 is in flight while chunk c
 // is contracted.
 template <int N, int J, int LDG> struct CoreStream {
-  static constexpr int D = N - 1;
-  static constexpr int NC = D == 3 ? J : J * J;       // chunks per pass over the core
+  static constexpr int NC = N == 4 ? J : J * J;       // chunks per pass over the core (N = 4 or 5)
   static constexpr size_t CH = (size_t)J * J * LDG;  // values per chunk
 };
 
