@@ -15,6 +15,7 @@ from .tucker import (  # noqa: F401
     plan_partition,
     coo_from_arrays,
     create_tensor_blocks,
+    release_cached_memory,
     generate,
     generate_planted,
     parse_buffer,
@@ -26,6 +27,6 @@ from .tucker import (  # noqa: F401
 
 __all__ = [
     "GTKError", "LIB_PATH", "Batch", "BlockedTensor", "Coo", "checkpoint_info", "coo_from_arrays",
-    "create_tensor_blocks", "device_memory", "generate", "generate_planted", "parse_buffer", "parse_from_file",
+    "create_tensor_blocks", "release_cached_memory", "device_memory", "generate", "generate_planted", "parse_buffer", "parse_from_file",
     "plan_partition", "tucker_decomposition", "WarmStart", "ws_features",
 ]

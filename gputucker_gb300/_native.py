@@ -116,6 +116,7 @@ SIGNATURES = {
     "gtk_plan_partition": (C.c_int, [C.c_int, U32P, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_uint64,
                                      C.POINTER(Plan)]),
     "gtk_device_memory": (C.c_int, [C.c_int, U64P, U64P]),
+    "gtk_release_cached_memory": (None, []),
     "gtk_checkpoint_save": (C.c_int, [P, C.c_char_p, C.POINTER(C.c_double), C.c_int]),
     "gtk_checkpoint_load": (C.c_int, [P, C.c_char_p, C.POINTER(C.c_double), C.c_int, C.POINTER(C.c_int)]),
     "gtk_checkpoint_info": (C.c_int, [C.c_char_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int), U32P,

@@ -7,6 +7,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -67,18 +68,104 @@ int ensure_norm_ref(DevTensor &t) {
   return 0;
 }
 
+namespace {
+struct CachedBlock {
+  int dev;
+  size_t bytes;
+  void *p;
+};
+std::mutex g_cache_mu;
+std::vector<CachedBlock> g_cache;
+uint64_t g_cache_cap[64] = {};  // half of each device's memory, read once
+
+uint64_t cache_cap(int dev) {
+  if (dev < 0 || dev >= 64) return 0;
+  if (!g_cache_cap[dev]) {
+    size_t f = 0, total = 0;
+    if (cudaMemGetInfo(&f, &total) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    g_cache_cap[dev] = total / 2;
+  }
+  return g_cache_cap[dev];
+}
+}  // namespace
+
+void *dev_alloc(int dev, size_t bytes) {
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    for (size_t i = 0; i < g_cache.size(); ++i)
+      if (g_cache[i].dev == dev && g_cache[i].bytes == bytes) {
+        void *p = g_cache[i].p;
+        g_cache.erase(g_cache.begin() + (long)i);
+        return p;
+      }
+  }
+  void *p = nullptr;
+  if (cudaMalloc(&p, bytes) == cudaSuccess) return p;
+  cudaGetLastError();
+  dev_cache_clear(dev);  // memory held by the cache goes back to the driver, then once more
+  if (cudaMalloc(&p, bytes) == cudaSuccess) return p;
+  cudaGetLastError();
+  return nullptr;
+}
+
+void dev_free(int dev, void *p, size_t bytes) {
+  if (!p) return;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    uint64_t held = 0;
+    for (const CachedBlock &b : g_cache)
+      if (b.dev == dev) held += b.bytes;
+    if (held + bytes <= cache_cap(dev)) {
+      g_cache.push_back({dev, bytes, p});
+      return;
+    }
+  }
+  cudaFree(p);
+}
+
+uint64_t dev_cached_bytes(int dev) {
+  std::lock_guard<std::mutex> lock(g_cache_mu);
+  uint64_t held = 0;
+  for (const CachedBlock &b : g_cache)
+    if (b.dev == dev) held += b.bytes;
+  return held;
+}
+
+void dev_cache_clear(int dev) {
+  std::vector<CachedBlock> out;
+  {
+    std::lock_guard<std::mutex> lock(g_cache_mu);
+    for (size_t i = 0; i < g_cache.size();) {
+      if (dev < 0 || g_cache[i].dev == dev) {
+        out.push_back(g_cache[i]);
+        g_cache.erase(g_cache.begin() + (long)i);
+      } else {
+        ++i;
+      }
+    }
+  }
+  int cur = 0;
+  cudaGetDevice(&cur);
+  for (const CachedBlock &b : out) {
+    cudaSetDevice(b.dev);
+    cudaFree(b.p);
+  }
+  cudaSetDevice(cur);
+  cudaGetLastError();
+}
+
 int dalloc(DevTensor &t, void **p, size_t bytes) {
   if (bytes < 16) bytes = 16;
   bytes = (bytes + 255) / 256 * 256;
   uint64_t cap = memory_cap();
   if (cap && t.bytes + bytes > cap)
     return fail(GTK_ERR_OOM, "device memory cap (GTK_DEVICE_MEMORY_CAP) exceeded");
-  cudaError_t e = cudaMalloc(p, bytes);
-  if (e != cudaSuccess) {
-    cudaGetLastError();
-    return fail(GTK_ERR_OOM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
-  }
-  t.allocs.push_back(*p);
+  *p = dev_alloc(t.dev, bytes);
+  if (!*p) return fail(GTK_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+  t.allocs.push_back({*p, bytes});
   t.bytes += bytes;
   return 0;
 }
@@ -87,7 +174,7 @@ static void release(DevTensor &t) {
   if (t.dev >= 0) cudaSetDevice(t.dev);
   if (t.stream) cudaStreamSynchronize(t.stream);
   drop_graph(t);
-  for (void *p : t.allocs) cudaFree(p);
+  for (const auto &a : t.allocs) dev_free(t.dev, a.first, a.second);
   t.allocs.clear();
   if (t.tev0) cudaEventDestroy(t.tev0);
   if (t.tev1) cudaEventDestroy(t.tev1);

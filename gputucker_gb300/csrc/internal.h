@@ -6,6 +6,7 @@
 
 #include <cstdint>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "gputucker_gb300.h"
@@ -170,12 +171,21 @@ struct DevTensor {
   uint64_t prof_n[4] = {};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
 
-  std::vector<void *> allocs;
+  std::vector<std::pair<void *, size_t>> allocs;  // device blocks of the handle and their sizes
   uint64_t bytes = 0;
 };
 
 // device memory helpers (api.cpp)
 int dalloc(DevTensor &t, void **p, size_t bytes);
+// Process-wide cache of device blocks: a freed block is kept (up to half of its
+// device's memory) and handed back to the next request of the same size on that
+// device, so that repeated handles of one shape neither unmap nor map memory.
+// dev_alloc: nullptr on failure (after clearing the cache and retrying once);
+// dev_free: the work using p must have finished.
+void *dev_alloc(int dev, size_t bytes);
+void dev_free(int dev, void *p, size_t bytes);
+uint64_t dev_cached_bytes(int dev);
+void dev_cache_clear(int dev);  // dev < 0: every device
 
 // partition.cu
 int build_partition(DevTensor &t, const gtk_coo &coo);

@@ -493,19 +493,19 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
     dm.P[k] = k < N ? t.P[k] : 1;
   }
   // temporaries, freed at the end
-  std::vector<void *> tmp;
+  // temporaries from the process-wide block cache (a repeated create of one
+  // shape reuses them), returned to it at the end
+  std::vector<std::pair<void *, size_t>> tmp;
   auto talloc = [&](void **p, size_t bytes) -> int {
-    cudaError_t e = cudaMalloc(p, bytes < 16 ? 16 : bytes);
-    if (e != cudaSuccess) {
-      cudaGetLastError();
-      return fail(GTK_ERR_OOM, std::string("device allocation of temporaries failed: ") + cudaGetErrorString(e));
-    }
-    tmp.push_back(*p);
+    bytes = (std::max<size_t>(bytes, 16) + 255) / 256 * 256;
+    *p = dev_alloc(t.dev, bytes);
+    if (!*p) return fail(GTK_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes of temporaries failed");
+    tmp.push_back({*p, bytes});
     return 0;
   };
   auto cleanup = [&]() {
     cudaStreamSynchronize(s);
-    for (void *p : tmp) cudaFree(p);
+    for (const auto &b : tmp) dev_free(t.dev, b.first, b.second);
   };
 #define TRY(x)          \
   do {                  \
@@ -543,17 +543,13 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
   // them the gathers read the coordinate arrays one by one
   uint4 *rin = nullptr, *rblk = nullptr;
   if (N <= kRecMaxOrder && n) {
-    if (cudaMalloc((void **)&rin, n * 32) == cudaSuccess) {
-      tmp.push_back(rin);
-      if (cudaMalloc((void **)&rblk, n * 32) == cudaSuccess) {
-        tmp.push_back(rblk);
-      } else {
-        rblk = nullptr;
-      }
-    } else {
-      rin = nullptr;
+    const size_t rb = (n * 32 + 255) / 256 * 256;
+    rin = static_cast<uint4 *>(dev_alloc(t.dev, rb));
+    if (rin) {
+      tmp.push_back({rin, rb});
+      rblk = static_cast<uint4 *>(dev_alloc(t.dev, rb));
+      if (rblk) tmp.push_back({rblk, rb});
     }
-    cudaGetLastError();
     if (!rblk) rin = nullptr;
     if (rin) {
       k_pack_records<V><<<G, T, 0, s>>>(gin, dval, N, n, rin);

@@ -210,10 +210,12 @@ int gtk_device_memory(int device, uint64_t *free_bytes, uint64_t *total_bytes) {
   const cudaError_t e = cudaMemGetInfo(&f, &t);
   cudaSetDevice(cur);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
-  *free_bytes = f;
+  *free_bytes = f + dev_cached_bytes(device);  // blocks the library keeps cached are free for its own use
   *total_bytes = t;
   return 0;
 }
+
+void gtk_release_cached_memory(void) { dev_cache_clear(-1); }
 
 int gtk_checkpoint_save(gtk_tensor *t, const char *path, const double *fits, int nfits) {
   if (!t || !path || nfits < 0 || (nfits > 0 && !fits)) return fail(GTK_ERR_ARG, "bad argument");

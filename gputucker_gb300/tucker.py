@@ -533,6 +533,12 @@ def ws_features(t: BlockedTensor, mode: int) -> np.ndarray:
     return out
 
 
+def release_cached_memory() -> None:
+    """Return the device blocks the library keeps cached to the driver
+    (gtk_release_cached_memory)."""
+    nat.load().gtk_release_cached_memory()
+
+
 def create_tensor_blocks(coo: Coo, partition_dims, rank: int, device: int = 0) -> BlockedTensor:
     """CreateTensorBlocks + AssignIndicesOfEachBlock on the GPU (gtk_create_blocks)."""
     P = np.ascontiguousarray(partition_dims, dtype=np.uint32)

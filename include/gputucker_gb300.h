@@ -210,6 +210,13 @@ typedef struct gtk_plan {
 int gtk_plan_partition(int order, const uint32_t *dims, uint64_t nnz, int rank, int dtype, int gpu_count,
                        uint64_t gpu_mem_bytes, gtk_plan *out);
 int gtk_device_memory(int device, uint64_t *free_bytes, uint64_t *total_bytes);
+/* No reference counterpart.  Device blocks freed by gtk_destroy and by the
+ * partition's temporaries stay cached in the process (up to half of each
+ * device's memory) and serve the next requests of the same size, so repeated
+ * handles of one shape neither unmap nor map memory; gtk_device_memory counts
+ * them as free, an allocation that fails clears the cache and retries, and this
+ * call returns every cached block to the driver. */
+void gtk_release_cached_memory(void);
 
 /* ---- checkpoint ---------------------------------------------------------
  * No reference counterpart.  gtk_checkpoint_save writes the factors, the core

@@ -183,3 +183,21 @@ def test_graph_replay_matches_eager(prec):
         for n in range(4):
             te.set_factor(n, tg.get_factor(n))
         assert abs(te.sweep() - tg.sweep()) <= 1e-6
+
+
+def test_cached_device_blocks_are_reused_cleanly():
+    """A handle created after another of the same shape was destroyed gets the
+    cached blocks back (stale contents): its sweeps equal the first handle's; the
+    cached bytes count as free, and releasing them returns them to the driver."""
+    coo = gtk.generate(4, [3000] * 4, 400_000, "zipf", 1.1, "uniform", "f32", seed=3)
+    fits = []
+    for _ in range(2):
+        with gtk.create_tensor_blocks(coo, [2, 2, 2, 2], 8) as t:
+            t.init_random(1, 0)
+            t.set_precision("bf16")
+            fits.append([t.sweep() for _ in range(2)])
+    np.testing.assert_allclose(fits[0], fits[1], rtol=0, atol=1e-6)  # up to the order of FP64 atomic adds
+    free_cached, total = gtk.device_memory()
+    gtk.release_cached_memory()
+    free_after, _ = gtk.device_memory()
+    assert abs(free_after - free_cached) <= total // 100, (free_cached, free_after)
