@@ -24,6 +24,7 @@
 #include <cstring>
 #include <vector>
 
+#include "blocks.cuh"
 #include "internal.h"
 
 namespace gtk {
@@ -41,18 +42,6 @@ struct ModePtrs {
   uint64_t stride[kMaxOrder];      // block id = sum_k c_k * stride[k], last mode fastest
 };
 
-// block of block-major position t: the last b with blk_ptr[b] <= t
-__device__ __forceinline__ uint32_t block_of(const uint64_t *__restrict__ blk_ptr, uint32_t nblk, uint64_t t) {
-  uint32_t lo = 0, hi = nblk;  // blk_ptr[lo] <= t < blk_ptr[hi]
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) / 2;
-    if (blk_ptr[mid] <= t)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
-}
 
 __device__ __forceinline__ uint32_t global_row(const ModePtrs &m, int k, uint32_t b, uint64_t t) {
   const uint32_t c = (uint32_t)((b / m.stride[k]) % m.P[k]);

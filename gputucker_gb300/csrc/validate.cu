@@ -18,6 +18,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "blocks.cuh"
 #include "internal.h"
 
 namespace gtk {
@@ -27,18 +28,6 @@ constexpr int kChecks = GTK_VALIDATE_CHECKS;
 
 __device__ __forceinline__ void bump(unsigned long long *cnt, int check, unsigned long long n) {
   if (n) atomicAdd(cnt + check, n);
-}
-
-__device__ __forceinline__ uint32_t block_of(const uint64_t *__restrict__ blk_ptr, uint32_t nblk, uint64_t t) {
-  uint32_t lo = 0, hi = nblk;
-  while (hi - lo > 1) {
-    const uint32_t mid = (lo + hi) / 2;
-    if (blk_ptr[mid] <= t)
-      lo = mid;
-    else
-      hi = mid;
-  }
-  return lo;
 }
 
 __global__ void k_check_below(const uint32_t *__restrict__ a, uint64_t n, uint32_t limit, int check,
