@@ -81,8 +81,13 @@ uint64_t g_cache_cap[64] = {};  // half of each device's memory, read once
 uint64_t cache_cap(int dev) {
   if (dev < 0 || dev >= 64) return 0;
   if (!g_cache_cap[dev]) {
+    // the total memory of `dev` itself, whichever device is current
+    int cur = -1;
     size_t f = 0, total = 0;
-    if (cudaMemGetInfo(&f, &total) != cudaSuccess) {
+    const bool ok = cudaGetDevice(&cur) == cudaSuccess && cudaSetDevice(dev) == cudaSuccess &&
+                    cudaMemGetInfo(&f, &total) == cudaSuccess;
+    if (cur >= 0) cudaSetDevice(cur);
+    if (!ok) {
       cudaGetLastError();
       return 0;
     }
@@ -109,6 +114,18 @@ void *dev_alloc(int dev, size_t bytes) {
   if (cudaMalloc(&p, bytes) == cudaSuccess) return p;
   cudaGetLastError();
   return nullptr;
+}
+
+cudaError_t malloc_retry(void **p, size_t bytes) {
+  *p = nullptr;
+  cudaError_t e = cudaMalloc(p, bytes);
+  if (e != cudaErrorMemoryAllocation) return e;
+  cudaGetLastError();
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return e;
+  if (dev_cached_bytes(dev) == 0) return e;
+  dev_cache_clear(dev);
+  return cudaMalloc(p, bytes);
 }
 
 void dev_free(int dev, void *p, size_t bytes) {
@@ -684,12 +701,11 @@ int gtk_compute_delta(gtk_tensor *t, int mode, void *delta) {
   GTK_GUARD_BEGIN
   const size_t bytes = t->nnz * (size_t)t->J * t->vsize;
   if (!bytes) return 0;
-  void *d = nullptr;
-  GTK_CUDA(cudaMalloc(&d, bytes));
-  int rc = run_delta(*t, mode, d);
-  if (!rc) rc = ck(cudaMemcpyAsync(delta, d, bytes, cudaMemcpyDeviceToHost, t->stream), "delta readback");
+  DevBuf d;
+  GTK_CUDA(d.alloc(bytes));
+  int rc = run_delta(*t, mode, d.p);
+  if (!rc) rc = ck(cudaMemcpyAsync(delta, d.p, bytes, cudaMemcpyDeviceToHost, t->stream), "delta readback");
   if (!rc) rc = ck(cudaStreamSynchronize(t->stream), "sync");
-  cudaFree(d);
   return rc;
   GTK_GUARD_END
 }
@@ -701,10 +717,15 @@ int gtk_profile_enable(gtk_tensor *t, int on) {
 }
 
 int gtk_profile_read(gtk_tensor *t, int kind, double *ms, uint64_t *launches) {
-  if (!t || kind < 0 || kind > 4) return fail(GTK_ERR_ARG, "bad argument");
+  if (!t || kind < 0 || kind > 6) return fail(GTK_ERR_ARG, "bad argument");
   if (kind == 4) {  // kernels launched by the sweep entry points since the last reset
     if (ms) *ms = 0;
     if (launches) *launches = t->launches;
+    return 0;
+  }
+  if (kind >= 5) {  // phases of gtk_create_blocks
+    if (ms) *ms = kind == 5 ? t->create_upload_ms : t->create_kernels_ms;
+    if (launches) *launches = 0;
     return 0;
   }
   if (int rc = set_dev(t)) return rc;

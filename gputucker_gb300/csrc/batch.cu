@@ -213,7 +213,7 @@ int gtk_autotune(gtk_tensor *t, int *variant) {
       cands.push_back(kVarSpec1);
       const size_t bytes = t->rows[0] * (size_t)t->ldf * t->vsize;
       void *save = nullptr;
-      GTK_CUDA(cudaMalloc(&save, bytes));
+      GTK_CUDA(malloc_retry(&save, bytes));
       int rc = ck(cudaMemcpyAsync(save, t->fac[0], bytes, cudaMemcpyDeviceToDevice, t->stream), "save");
       const bool prof = t->prof;
       t->prof = false;
@@ -281,8 +281,8 @@ int gtk_batch_create(gtk_tensor *const *tensors, int count, gtk_batch **out) {
     tab[count + i] = b->ts[i]->status;
   }
   const size_t out_bytes = (size_t)count * (sizeof(double) + sizeof(int));
-  if (int rc = ck(cudaMalloc(&b->d_tab, tab.size() * sizeof(void *)), "cudaMalloc")) return bail(rc);
-  if (int rc = ck(cudaMalloc(&b->d_out, out_bytes), "cudaMalloc")) return bail(rc);
+  if (int rc = ck(malloc_retry(&b->d_tab, tab.size() * sizeof(void *)), "cudaMalloc")) return bail(rc);
+  if (int rc = ck(malloc_retry(&b->d_out, out_bytes), "cudaMalloc")) return bail(rc);
   if (int rc = ck(cudaMemcpy(b->d_tab, tab.data(), tab.size() * sizeof(void *), cudaMemcpyHostToDevice), "H2D"))
     return bail(rc);
   b->h_out.resize(out_bytes);

@@ -212,9 +212,9 @@ template <class V> int update_core_impl(DevTensor &t, int iters, int *iters_run,
   const unsigned grid = (unsigned)(nranges * nchunks);
 
   CoreScratch sc;
-  GTK_CUDA(cudaMalloc(&sc.delta, nnz * (size_t)J * sizeof(V)));
-  GTK_CUDA(cudaMalloc(&sc.y, nnz * sizeof(V)));
-  GTK_CUDA(cudaMalloc((void **)&sc.acc, M * sizeof(double)));
+  GTK_CUDA(malloc_retry(&sc.delta, nnz * (size_t)J * sizeof(V)));
+  GTK_CUDA(malloc_retry(&sc.y, nnz * sizeof(V)));
+  GTK_CUDA(malloc_retry((void **)&sc.acc, M * sizeof(double)));
   std::vector<double> hacc(M);
   // Phi^T w for device weights w (block-major order)
   auto phi_t = [&](const V *w, std::vector<double> &res) -> int {

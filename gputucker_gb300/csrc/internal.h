@@ -169,6 +169,9 @@ struct DevTensor {
   bool prof = false;
   double prof_ms[4] = {};
   uint64_t prof_n[4] = {};
+  // gtk_create_blocks, CUDA events on the stream: host-to-device upload of the
+  // COO, then the partition and segmenting kernels (ms)
+  double create_upload_ms = 0, create_kernels_ms = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
 
   std::vector<std::pair<void *, size_t>> allocs;  // device blocks of the handle and their sizes
@@ -186,6 +189,25 @@ void *dev_alloc(int dev, size_t bytes);
 void dev_free(int dev, void *p, size_t bytes);
 uint64_t dev_cached_bytes(int dev);
 void dev_cache_clear(int dev);  // dev < 0: every device
+// cudaMalloc on the current device; when it fails, the blocks the cache holds
+// for that device go back to the driver and the allocation is tried once more
+// (so memory this process keeps cached never makes an allocation fail)
+cudaError_t malloc_retry(void **p, size_t bytes);
+template <class T> inline cudaError_t malloc_retry(T **p, size_t bytes) {
+  return malloc_retry(reinterpret_cast<void **>(p), bytes);
+}
+// a device buffer freed (cudaFree) on every return path
+struct DevBuf {
+  void *p = nullptr;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  cudaError_t alloc(size_t bytes) { return malloc_retry(&p, bytes); }
+  template <class T> T *as() const { return static_cast<T *>(p); }
+};
 
 // partition.cu
 int build_partition(DevTensor &t, const gtk_coo &coo);

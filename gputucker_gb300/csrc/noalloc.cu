@@ -1,12 +1,12 @@
 // noalloc.cu -- the reconstruction error of caller-owned device data, without
 // allocating anything.
 //
-// Who needs it: code that cannot call cudaMalloc where it runs -- work being
-// recorded into a CUDA graph by stream capture (allocation calls are not
-// allowed while a stream is capturing), latency-critical loops that must not
-// touch the allocator, and hosts whose device memory belongs to another
-// runtime's pool.  They hand in device pointers to their own tensor, factors and
-// core and get the sum of squared errors back in device memory.
+// Who needs it: code that cannot call cudaMalloc where it runs --
+// latency-critical loops that must not touch the allocator (cudaMalloc and
+// cudaFree synchronise the device and cost milliseconds), and hosts whose device
+// memory belongs to another runtime's pool or is capped by it.  They hand in
+// device pointers to their own tensor, factors and core and get the sum of
+// squared errors back in device memory.
 //
 // The kernel is the generic reconstruction kernel of sweep.cu (x_hat =
 // delta . a[i] with delta the staged contraction of the core with the other

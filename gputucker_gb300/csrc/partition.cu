@@ -516,6 +516,17 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
     }                   \
   } while (0)
 
+  // phase timers (upload, kernels), read back at the end
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  struct EvGuard {
+    cudaEvent_t *e;
+    ~EvGuard() {
+      for (int i = 0; i < 3; ++i)
+        if (e[i]) cudaEventDestroy(e[i]);
+    }
+  } ev_guard{ev};
+  for (auto &e : ev) TRY(ck(cudaEventCreate(&e), "cudaEventCreate"));
+  TRY(ck(cudaEventRecord(ev[0], s), "cudaEventRecord"));
   // upload COO
   Ptrs gin;
   for (int k = 0; k < N; ++k) {
@@ -529,6 +540,7 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
   V *dval = reinterpret_cast<V *>(t.val_in);
   if (n) TRY(ck(cudaMemcpyAsync(dval, coo.values(), n * sizeof(V), cudaMemcpyHostToDevice, s), "upload values"));
 
+  TRY(ck(cudaEventRecord(ev[1], s), "cudaEventRecord"));
   SortScratch sc;
   const uint64_t ntiles = (n + kRsTile - 1) / kRsTile;
   TRY(talloc((void **)&sc.k2, n * 4));
@@ -626,7 +638,15 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
   }
   t.h_blk_ptr.resize(t.nblk + 1);
   TRY(ck(cudaMemcpyAsync(t.h_blk_ptr.data(), t.blk_ptr, (t.nblk + 1) * 8, cudaMemcpyDeviceToHost, s), "blk_ptr"));
+  TRY(ck(cudaEventRecord(ev[2], s), "cudaEventRecord"));
   TRY(ck(cudaStreamSynchronize(s), "partition sync"));
+  {
+    float up = 0, kern = 0;
+    TRY(ck(cudaEventElapsedTime(&up, ev[0], ev[1]), "cudaEventElapsedTime"));
+    TRY(ck(cudaEventElapsedTime(&kern, ev[1], ev[2]), "cudaEventElapsedTime"));
+    t.create_upload_ms = up;
+    t.create_kernels_ms = kern;
+  }
   cleanup();
 #undef TRY
   return 0;

@@ -1405,7 +1405,7 @@ int run_row_stats(DevTensor &t, int mode, uint32_t *max_count) {
   *max_count = 0;
   if (!t.nnz) return 0;
   uint32_t *cnt = nullptr;
-  GTK_CUDA(cudaMalloc(&cnt, (t.rows[mode] + 1) * 4));
+  GTK_CUDA(malloc_retry(&cnt, (t.rows[mode] + 1) * 4));
   int rc = ck(cudaMemsetAsync(cnt, 0, (t.rows[mode] + 1) * 4, t.stream), "memset");
   if (!rc) {
     k_row_count<<<t.num_sms * 8, 256, 0, t.stream>>>(t.vidx[mode][mode], t.nnz, cnt);

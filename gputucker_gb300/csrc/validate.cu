@@ -81,8 +81,9 @@ __global__ void k_check_finite(const V *__restrict__ a, uint64_t rows, int cols,
 }
 
 template <class V> int validate_impl(DevTensor &t, uint64_t *out) {
-  unsigned long long *cnt = nullptr;
-  GTK_CUDA(cudaMalloc(&cnt, kChecks * sizeof(unsigned long long)));
+  DevBuf cbuf;  // freed on every return path
+  GTK_CUDA(cbuf.alloc(kChecks * sizeof(unsigned long long)));
+  unsigned long long *cnt = cbuf.as<unsigned long long>();
   GTK_CUDA(cudaMemsetAsync(cnt, 0, kChecks * sizeof(unsigned long long), t.stream));
   const unsigned g = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((t.nnz + 255) / 256, (uint64_t)t.num_sms * 8));
   const uint32_t nblk = (uint32_t)t.nblk;
@@ -107,7 +108,6 @@ template <class V> int validate_impl(DevTensor &t, uint64_t *out) {
   unsigned long long h[kChecks];
   GTK_CUDA(cudaMemcpyAsync(h, cnt, sizeof(h), cudaMemcpyDeviceToHost, t.stream));
   GTK_CUDA(cudaStreamSynchronize(t.stream));
-  cudaFree(cnt);
   for (int c = 0; c < kChecks; ++c) out[c] = h[c];
   // block pointers: the host copy the partition read back, and the device array against it
   std::vector<uint64_t> bp(t.nblk + 1);

@@ -367,7 +367,7 @@ int mode_features(gtk_tensor *t, int n, float *d_feat) {
   std::vector<double *> bufs;
   auto alloc = [&](size_t n) -> double * {
     void *p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess) return nullptr;
+    if (malloc_retry(&p, std::max<size_t>(n, 1) * sizeof(double)) != cudaSuccess) return nullptr;
     bufs.push_back(static_cast<double *>(p));
     return static_cast<double *>(p);
   };
@@ -452,7 +452,7 @@ int ensure_batch(gtk_ws *m, int B) {
     }
   const size_t sz[] = {(size_t)B * m->F, (size_t)B * m->J, (size_t)B * m->H, (size_t)B * m->H,
                        (size_t)B * m->J, (size_t)B * m->J, (size_t)B * m->H, (size_t)B * m->H};
-  for (int i = 0; i < 8; ++i) GTK_CUDA(cudaMalloc((void **)ps[i], sz[i] * sizeof(float)));
+  for (int i = 0; i < 8; ++i) GTK_CUDA(malloc_retry((void **)ps[i], sz[i] * sizeof(float)));
   m->bcap = B;
   return 0;
 }
@@ -513,10 +513,10 @@ int gtk_ws_create(int order, int rank, int hidden, uint64_t seed, int device, gt
   if (int rc = ck(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking), "stream")) return bail(rc);
   float **ps[] = {&m->w, &m->g, &m->m1, &m->m2};
   for (float **p : ps)
-    if (int rc = ck(cudaMalloc((void **)p, m->np * sizeof(float)), "cudaMalloc")) return bail(rc);
-  if (int rc = ck(cudaMalloc((void **)&m->d_fmean, m->F * 4), "cudaMalloc")) return bail(rc);
-  if (int rc = ck(cudaMalloc((void **)&m->d_fstd, m->F * 4), "cudaMalloc")) return bail(rc);
-  if (int rc = ck(cudaMalloc((void **)&m->loss, 8), "cudaMalloc")) return bail(rc);
+    if (int rc = ck(malloc_retry((void **)p, m->np * sizeof(float)), "cudaMalloc")) return bail(rc);
+  if (int rc = ck(malloc_retry((void **)&m->d_fmean, m->F * 4), "cudaMalloc")) return bail(rc);
+  if (int rc = ck(malloc_retry((void **)&m->d_fstd, m->F * 4), "cudaMalloc")) return bail(rc);
+  if (int rc = ck(malloc_retry((void **)&m->loss, 8), "cudaMalloc")) return bail(rc);
   // He-uniform weights, zero biases, from a seeded host generator
   std::vector<float> w(m->np, 0.f);
   uint64_t st = seed * 0x9E3779B97F4A7C15ull + 1;
@@ -672,7 +672,7 @@ int gtk_ws_features(gtk_tensor *t, int mode, float *out) {
   GTK_CUDA(cudaSetDevice(t->dev));
   const int F = ws_nfeat(t->N);
   float *d = nullptr;
-  GTK_CUDA(cudaMalloc(&d, std::max<size_t>(1, t->rows[mode] * F) * 4));
+  GTK_CUDA(malloc_retry(&d, std::max<size_t>(1, t->rows[mode] * F) * 4));
   int rc = mode_features(t, mode, d);
   if (!rc) rc = ck(cudaMemcpy(out, d, t->rows[mode] * F * 4, cudaMemcpyDeviceToHost), "D2H");
   cudaFree(d);
@@ -690,7 +690,7 @@ int gtk_ws_add_example(gtk_ws *m, gtk_tensor *t) {
     const uint64_t rows = t->dims[n];
     std::vector<float> feat((size_t)t->rows[n] * m->F);
     float *d = nullptr;
-    GTK_CUDA(cudaMalloc(&d, std::max<size_t>(1, feat.size()) * 4));
+    GTK_CUDA(malloc_retry(&d, std::max<size_t>(1, feat.size()) * 4));
     int rc = mode_features(t, n, d);
     if (!rc) rc = ck(cudaMemcpy(feat.data(), d, feat.size() * 4, cudaMemcpyDeviceToHost), "D2H");
     std::vector<uint32_t> pick;
@@ -701,8 +701,8 @@ int gtk_ws_add_example(gtk_ws *m, gtk_tensor *t) {
       if (m->ex_n + k > m->ex_cap) {  // grow the example arrays
         const uint64_t cap = std::max<uint64_t>(m->ex_n + k, m->ex_cap * 2);
         float *nf = nullptr, *nt = nullptr;
-        rc = ck(cudaMalloc(&nf, cap * m->F * 4), "cudaMalloc");
-        if (!rc) rc = ck(cudaMalloc(&nt, cap * m->J * 4), "cudaMalloc");
+        rc = ck(malloc_retry(&nf, cap * m->F * 4), "cudaMalloc");
+        if (!rc) rc = ck(malloc_retry(&nt, cap * m->J * 4), "cudaMalloc");
         if (!rc && m->ex_n) rc = ck(cudaMemcpy(nf, m->ex_f, m->ex_n * m->F * 4, cudaMemcpyDeviceToDevice), "D2D");
         if (!rc && m->ex_n) rc = ck(cudaMemcpy(nt, m->ex_t, m->ex_n * m->J * 4, cudaMemcpyDeviceToDevice), "D2D");
         if (rc) {
@@ -717,7 +717,7 @@ int gtk_ws_add_example(gtk_ws *m, gtk_tensor *t) {
         }
       }
       uint32_t *dp = nullptr;
-      if (!rc) rc = ck(cudaMalloc(&dp, k * 4), "cudaMalloc");
+      if (!rc) rc = ck(malloc_retry(&dp, k * 4), "cudaMalloc");
       if (!rc) rc = ck(cudaMemcpy(dp, pick.data(), k * 4, cudaMemcpyHostToDevice), "H2D");
       if (!rc) {
         k_gather_feat<<<grid_for(k * m->F), kWsThreads, 0, m->stream>>>(d, dp, k, m->F, m->ex_f + m->ex_n * m->F);
@@ -791,7 +791,7 @@ int gtk_ws_train(gtk_ws *m, int steps, int batch, float lr, double *final_loss) 
   }
   if (int rc = ensure_batch(m, batch)) return rc;
   uint64_t *idx = nullptr;
-  GTK_CUDA(cudaMalloc(&idx, (size_t)batch * 8));
+  GTK_CUDA(malloc_retry(&idx, (size_t)batch * 8));
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   int rc = 0;
   double l = 0;
@@ -824,9 +824,9 @@ int gtk_ws_apply(gtk_ws *m, gtk_tensor *t) {
   for (int n = 0; n < t->N; ++n) {
     const uint64_t rows = t->rows[n];
     float *d = nullptr, *z = nullptr, *y = nullptr;
-    int rc = ck(cudaMalloc(&d, std::max<uint64_t>(1, rows) * m->F * 4), "cudaMalloc");
-    if (!rc) rc = ck(cudaMalloc(&z, std::max<uint64_t>(1, rows) * m->F * 4), "cudaMalloc");
-    if (!rc) rc = ck(cudaMalloc(&y, std::max<uint64_t>(1, rows) * m->J * 4), "cudaMalloc");
+    int rc = ck(malloc_retry(&d, std::max<uint64_t>(1, rows) * m->F * 4), "cudaMalloc");
+    if (!rc) rc = ck(malloc_retry(&z, std::max<uint64_t>(1, rows) * m->F * 4), "cudaMalloc");
+    if (!rc) rc = ck(malloc_retry(&y, std::max<uint64_t>(1, rows) * m->J * 4), "cudaMalloc");
     if (!rc) rc = mode_features(t, n, d);
     if (!rc) {
       k_standardise<<<grid_for(rows * m->F), kWsThreads, 0, t->stream>>>(d, z, rows, m->F, m->d_fmean, m->d_fstd);

@@ -310,9 +310,10 @@ int gtk_ws_predict(gtk_ws *m, const float *x, int batch, float *y);
 
 /* ---- no device allocation ----------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
- * memory where they run -- work recorded into a CUDA graph by stream capture,
- * allocator-free latency-critical loops, device memory owned by another
- * runtime's pool: the sum of squared reconstruction errors sum_t (x_t - x_hat_t)^2
+ * memory where they run -- latency-critical loops that must not touch the
+ * allocator (cudaMalloc/cudaFree synchronise the device and take milliseconds),
+ * hosts whose device memory belongs to another runtime's pool or is capped by
+ * it: the sum of squared reconstruction errors sum_t (x_t - x_hat_t)^2
  * of caller-owned device data, written to d_err (one double in device memory)
  * by kernels enqueued on `stream` (a cudaStream_t; NULL = the legacy default
  * stream).  FP32 data: d_idx[n] -> nnz 0-based coordinates of mode n, d_vals ->
@@ -354,7 +355,9 @@ int gtk_write_text(const gtk_coo *coo, const char *path);
 /* Per-kernel device time accumulated with CUDA events on the handle's stream
  * while enabled.  kind: 0 delta+gram, 1 solve, 2 fit, 3 whole sweeps replayed
  * from a graph (gtk_set_graph); kind 4 reads the number of kernels the sweep
- * entry points launched (ms = 0). */
+ * entry points launched (ms = 0).  Kinds 5 and 6 read the phases of the
+ * handle's gtk_create_blocks, always recorded: 5 the host-to-device upload of
+ * the COO, 6 the partition and segmenting kernels (launches = 0). */
 int gtk_profile_enable(gtk_tensor *t, int on);
 int gtk_profile_read(gtk_tensor *t, int kind, double *ms, uint64_t *launches);
 int gtk_profile_reset(gtk_tensor *t);

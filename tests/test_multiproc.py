@@ -57,7 +57,7 @@ def test_reference_arm_under_torchrun_two_ranks():
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(port), os.path.join(ROOT, "bench.py"),
            "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0", "--nnz", "40000",
-           "--ref-sample", "4000"]
+           "--cpu-sample", "4000"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -65,3 +65,21 @@ def test_reference_arm_under_torchrun_two_ranks():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0 and d["n_gpus"] == 2
     assert d["cpu_baseline"]["kind"] == "port"
+
+
+def test_reference_arm_loads_no_product_library():
+    """The reference arm times the oracle port on a numpy-drawn sample: neither the
+    package nor its shared library may be loaded in that process."""
+    code = (
+        "import sys, json, bench\n"
+        "sys.argv = ['bench.py', '--impl', 'reference', '--steps', '1', '--warmup', '0', '--cpu-sample', '3000']\n"
+        "bench.main()\n"
+        "maps = open('/proc/self/maps').read()\n"
+        "assert 'libgputucker_gb300' not in maps, 'product library mapped'\n"
+        "assert 'gputucker_gb300' not in sys.modules, 'product package imported'\n"
+        "assert 'libgtk_oracle' in maps\n"
+    )
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, cwd=ROOT)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][0])
+    assert d["impl"] == "reference" and d["config"]["workload"] == "zipf4d_100M_rank10_P4"

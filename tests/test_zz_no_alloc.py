@@ -1,11 +1,12 @@
 """gtk_reconstruction_error_noalloc: the reconstruction error without any device allocation.
 
-For callers that cannot allocate device memory where they run (stream capture
-into a CUDA graph, allocator-free loops, memory owned by another runtime).  The
-entry point reads the caller's device arrays and keeps its scratch in a fixed
-device array of the library.  Checked against the existing entry point
-(gtk_reconstruction on a handle) on two calls in a row; the FP32 fits agree to
-the tolerance the FP32 tests use (1e-5).
+For callers that cannot allocate device memory where they run (latency-critical
+loops that must not touch the allocator, device memory owned or capped by
+another runtime's pool).  The entry point reads the caller's device arrays and
+keeps its scratch in a fixed device array of the library.  Checked on two calls
+in a row against the existing entry point (gtk_reconstruction on a handle) and
+against the FP64 oracle's error of the same factors and core; the FP32 fits
+agree to the tolerance the FP32 tests use (1e-5).
 
 The device buffers here come from torch (any allocator works: the entry point
 only needs device pointers).  This file sorts last so that a run stopping at the
@@ -19,7 +20,7 @@ import pytest
 
 import gputucker_gb300 as gtk
 from gputucker_gb300 import _native as nat
-from oracle_util import random_coo
+from oracle_util import Oracle, random_coo
 
 pytestmark = pytest.mark.gpu
 
@@ -49,6 +50,12 @@ def test_noalloc_error_matches_reconstruction(case):
         facs = [t.get_factor(n)[:dims[n]] for n in range(N)]
         core = t.get_core()
         fit_ref = t.reconstruction()
+        # the oracle's error of the same factors and core (FP64 arithmetic on the FP32 values)
+        ora = Oracle(1, idx, vals.astype(np.float64), dims, P, J)
+        for n in range(N):
+            ora.set_factor(n, t.get_factor(n).astype(np.float64))
+        ora.set_core(core.astype(np.float64))
+        fit_ora = ora.fit()["fit64"]
         d_idx = [_dev(torch, i) for i in idx]
         d_val = _dev(torch, vals)
         d_fac = [_dev(torch, f) for f in facs]
@@ -67,6 +74,7 @@ def test_noalloc_error_matches_reconstruction(case):
             err = float(d_err.item())
             fit = 1.0 - np.sqrt(err) / t.info.norm
             assert abs(fit - fit_ref) <= FIT_TOL, (call, fit, fit_ref)
+            assert abs(fit - fit_ora) <= FIT_TOL, (call, fit, fit_ora)
 
 
 def test_noalloc_rejects_core_beyond_scratch():
