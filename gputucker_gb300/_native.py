@@ -143,6 +143,7 @@ SIGNATURES = {
     "gtk_batch_destroy": (None, [P]),
     "gtk_profile_enable": (C.c_int, [P, C.c_int]),
     "gtk_profile_read": (C.c_int, [P, C.c_int, C.POINTER(C.c_double), U64P]),
+    "gtk_solve_counters": (C.c_int, [P, U64P, U64P, C.c_int]),
     "gtk_profile_reset": (C.c_int, [P]),
     "gtk_timer_begin": (C.c_int, [P]),
     "gtk_timer_end": (C.c_int, [P, C.POINTER(C.c_double)]),

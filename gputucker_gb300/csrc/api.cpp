@@ -444,6 +444,7 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
     if ((rc = ck(cudaMemsetAsync(t->corep[n], 0, (core_n / rank) * t->ldf * vs, t->stream), "memset"))) return bail(rc);
   }
   if ((rc = ck(cudaMemsetAsync(t->status, 0, 16, t->stream), "memset"))) return bail(rc);
+  if ((rc = ck(cudaMemsetAsync(t->nfallback, 0, 16, t->stream), "memset"))) return bail(rc);
   rc = build_partition(*t, *coo);
   if (rc) return bail(rc);
   *out = t;
@@ -708,6 +709,21 @@ int gtk_compute_delta(gtk_tensor *t, int mode, void *delta) {
   if (!rc) rc = ck(cudaStreamSynchronize(t->stream), "sync");
   return rc;
   GTK_GUARD_END
+}
+
+int gtk_solve_counters(gtk_tensor *t, uint64_t *fp64_rows, uint64_t *lu_rows, int reset) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (int rc = set_dev(t)) return rc;
+  unsigned int c[4] = {0, 0, 0, 0};
+  GTK_CUDA(cudaMemcpyAsync(c, t->nfallback, sizeof(c), cudaMemcpyDeviceToHost, t->stream));
+  GTK_CUDA(cudaStreamSynchronize(t->stream));
+  if (fp64_rows) *fp64_rows = c[2];
+  if (lu_rows) *lu_rows = c[3];
+  if (reset) {
+    GTK_CUDA(cudaMemsetAsync(t->nfallback + 2, 0, 8, t->stream));
+    GTK_CUDA(cudaStreamSynchronize(t->stream));
+  }
+  return 0;
 }
 
 int gtk_profile_enable(gtk_tensor *t, int on) {

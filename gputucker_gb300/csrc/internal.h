@@ -157,6 +157,8 @@ struct DevTensor {
   void *dstore = nullptr;       // [nnz][J] value_t, view order of the last mode
   uint32_t *fallback = nullptr; // rows re-solved by pivoted LU
   uint32_t *fallback64 = nullptr; // precision form: rows re-solved in FP64
+  // [0] rows of the current mode listed for LU, [1] for FP64 Cholesky;
+  // [2] FP64 and [3] LU rows since creation or gtk_solve_counters' last reset
   unsigned int *nfallback = nullptr;
   uint64_t launches = 0;        // kernels launched by the sweep entry points
   int variant = -1;             // update kernel: kVarAuto or one the autotuner picked

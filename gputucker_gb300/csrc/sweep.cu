@@ -460,6 +460,7 @@ __global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, con
       for (int j = 0; j < ldf; ++j) frow[j] = j < J ? (V)A[upk(j, J, J) * T] : V(0);
     } else {
       fallback[atomicAdd(nfallback, 1u)] = (uint32_t)row;
+      atomicAdd(nfallback + 3, 1u);  // running count of the handle (gtk_solve_counters)
     }
   }
 }
@@ -509,6 +510,7 @@ __global__ void k_solve_rows32(const double *__restrict__ gram, uint64_t rows, i
     }
     if (!ok || (umax / umin) * (umax / umin) > cond_max) {
       to_fp64[atomicAdd(n_to_fp64, 1u)] = (uint32_t)row;
+      atomicAdd(n_to_fp64 + 1, 1u);  // running count of the handle (gtk_solve_counters)
       continue;
     }
     for (int k = J - 1; k >= 0; --k) {  // U a = y, a kept in column J

@@ -323,6 +323,13 @@ class BlockedTensor:
         call("gtk_profile_read", self.handle, kind, C.byref(ms), C.byref(n))
         return ms.value, n.value
 
+    def solve_counters(self, reset: bool = False) -> tuple[int, int]:
+        """(rows re-solved in FP64 by the precision forms, rows solved by pivoted LU)
+        since creation or the last reset (gtk_solve_counters)."""
+        f, l = C.c_uint64(), C.c_uint64()
+        call("gtk_solve_counters", self.handle, C.byref(f), C.byref(l), 1 if reset else 0)
+        return f.value, l.value
+
     def profile_reset(self) -> None:
         call("gtk_profile_reset", self.handle)
 

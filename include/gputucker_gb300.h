@@ -351,6 +351,16 @@ int gtk_generate_planted(int order, const uint32_t *dims, uint64_t nnz, int plan
                          int dtype, uint64_t seed, gtk_coo **out);
 int gtk_write_text(const gtk_coo *coo, const char *path);
 
+/* ---- row-solve statistics ---------------------------------------------
+ * No reference counterpart (the reference inverts every B by LU in FP64,
+ * update.cuh:163-194).  Rows solved by a fallback since the handle was created
+ * or the counters were last reset: fp64_rows -- rows of the precision forms
+ * whose FP32 Cholesky showed a condition estimate (max u_kk / min u_kk)^2 above
+ * 1e5, or a non-positive pivot, and were re-solved by FP64 Cholesky; lu_rows --
+ * rows whose FP64 Cholesky met a non-positive pivot and were solved by LU with
+ * partial pivoting.  reset != 0 zeroes both after reading. */
+int gtk_solve_counters(gtk_tensor *t, uint64_t *fp64_rows, uint64_t *lu_rows, int reset);
+
 /* ---- timing ----------------------------------------------------------- */
 /* Per-kernel device time accumulated with CUDA events on the handle's stream
  * while enabled.  kind: 0 delta+gram, 1 solve, 2 fit, 3 whole sweeps replayed
