@@ -270,7 +270,7 @@ int generate(int N, const uint32_t *dims, uint64_t nnz, int index_dist, double z
   }
   // values
   const uint64_t vseed = splitmix(sseed);
-  std::vector<double> v(nnz);
+  HostVec<double> v(nnz);
   if (value_dist == GTK_VAL_PLANTED) {
     const int R = planted_rank;
     if (R < 1 || R > GTK_MAX_RANK) return fail(GTK_ERR_ARG, "planted rank must be 1..64");

@@ -5,6 +5,7 @@
 #include <nvtx3/nvToolsExt.h>
 
 #include <cstdint>
+#include <memory>
 #include <string>
 #include <utility>
 #include <vector>
@@ -88,14 +89,28 @@ struct GlibcRand {
 }  // namespace gtk
 
 // Host-side parsed tensor: one block of global 0-based coordinates.
+// std::allocator whose value-less construct leaves the element uninitialised:
+// resize() of a large host array costs no serial zeroing pass, and its pages are
+// first touched by the threads that fill them
+template <class T> struct NoInitAlloc : std::allocator<T> {
+  template <class U> struct rebind {
+    using other = NoInitAlloc<U>;
+  };
+  NoInitAlloc() = default;
+  template <class U> NoInitAlloc(const NoInitAlloc<U> &) noexcept {}
+  template <class U> void construct(U *p) noexcept { ::new ((void *)p) U; }
+  template <class U, class... A> void construct(U *p, A &&...a) { ::new ((void *)p) U(std::forward<A>(a)...); }
+};
+template <class T> using HostVec = std::vector<T, NoInitAlloc<T>>;
+
 struct gtk_coo {
   int N = 0;
   int dtype = GTK_F32;
   uint64_t nnz = 0;
   uint32_t dims[GTK_MAX_ORDER] = {};
-  std::vector<uint32_t> idx[GTK_MAX_ORDER];
-  std::vector<float> vf;
-  std::vector<double> vd;
+  HostVec<uint32_t> idx[GTK_MAX_ORDER];
+  HostVec<float> vf;
+  HostVec<double> vd;
   uint64_t draws = 0;  // rand() draws consumed by lines without a value
   bool pinned = false;
   const void *values() const { return dtype == GTK_F32 ? (const void *)vf.data() : (const void *)vd.data(); }

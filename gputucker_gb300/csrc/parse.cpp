@@ -17,6 +17,10 @@
 // memory; this includes empty lines, which the reference merges with the next
 // line) and a value token strtod cannot read (std::stod throws).
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
 #include <algorithm>
 #include <cerrno>
 #include <cstdio>
@@ -53,6 +57,72 @@ inline uint32_t parse_index(const char *s, const char *e) {
   return (uint32_t)strtoull(tok.c_str(), nullptr, 10);
 }
 
+// 10^0 .. 10^22: every one exactly representable in double
+constexpr double kPow10[23] = {1e0,  1e1,  1e2,  1e3,  1e4,  1e5,  1e6,  1e7,  1e8,  1e9,  1e10, 1e11,
+                               1e12, 1e13, 1e14, 1e15, 1e16, 1e17, 1e18, 1e19, 1e20, 1e21, 1e22};
+
+// The value token as strtod reads it, for the common decimal forms
+// [+-]digits[.digits][(e|E)[+-]digits] spanning the whole token.  Clinger's fast
+// path (W. D. Clinger, "How to read floating point numbers accurately", PLDI
+// 1990): with the significant digits m < 2^53 and the decimal exponent
+// |q| <= 22, m and 10^|q| are exact doubles, so one IEEE multiply or divide
+// gives the correctly rounded value -- the double strtod returns.  Anything else
+// (more digits, larger exponents, hex, inf/nan, trailing characters) returns
+// false and goes to strtod.
+inline bool parse_value_fast(const char *s, const char *e, double &out) {
+  const char *p = s;
+  bool neg = false;
+  if (p < e && (*p == '+' || *p == '-')) {
+    neg = *p == '-';
+    ++p;
+  }
+  uint64_t m = 0;
+  int sig = 0, q = 0;
+  bool digits = false;
+  for (; p < e && (unsigned)(*p - '0') <= 9u; ++p) {
+    digits = true;
+    if (m || *p != '0') {
+      if (++sig > 19) return false;
+      m = m * 10 + (unsigned)(*p - '0');
+    }
+  }
+  if (p < e && *p == '.') {
+    for (++p; p < e && (unsigned)(*p - '0') <= 9u; ++p) {
+      digits = true;
+      --q;
+      if (m || *p != '0') {
+        if (++sig > 19) return false;
+        m = m * 10 + (unsigned)(*p - '0');
+      }
+    }
+  }
+  if (!digits) return false;
+  if (p < e && (*p == 'e' || *p == 'E')) {
+    ++p;
+    bool eneg = false;
+    if (p < e && (*p == '+' || *p == '-')) {
+      eneg = *p == '-';
+      ++p;
+    }
+    if (p >= e) return false;
+    int x = 0;
+    for (; p < e && (unsigned)(*p - '0') <= 9u; ++p) {
+      if (x > 10000) return false;
+      x = x * 10 + (*p - '0');
+    }
+    q += eneg ? -x : x;
+  }
+  if (p != e) return false;
+  if (m == 0) {
+    out = neg ? -0.0 : 0.0;
+    return true;
+  }
+  if (m > (1ull << 53) || q < -22 || q > 22) return false;
+  const double v = q < 0 ? (double)m / kPow10[-q] : (double)m * kPow10[q];
+  out = neg ? -v : v;
+  return true;
+}
+
 struct Chunk {
   size_t begin = 0, end = 0;  // byte range, whole lines
   uint64_t lines = 0, first_line = 0;
@@ -60,6 +130,7 @@ struct Chunk {
   uint64_t err_line = UINT64_MAX;
   int err_code = 0;
   std::string err_msg;
+  std::vector<uint64_t> missing;  // lines without a value, in file order
 };
 
 }  // namespace
@@ -114,12 +185,12 @@ int parse_buffer(const char *buf, size_t len, int N, int dtype, uint32_t seed, g
   out->N = N;
   out->dtype = dtype;
   out->nnz = nnz;
-  for (int n = 0; n < N; ++n) out->idx[n].assign(nnz, 0);
+  // uninitialised: every entry is written below by the thread that parses its line
+  for (int n = 0; n < N; ++n) out->idx[n].resize(nnz);
   if (dtype == GTK_F32)
-    out->vf.assign(nnz, 0.f);
+    out->vf.resize(nnz);
   else
-    out->vd.assign(nnz, 0.0);
-  std::vector<unsigned char> missing(nnz, 0);
+    out->vd.resize(nnz);
 
   auto work = [&](unsigned c) {
     Chunk &k = ch[c];
@@ -145,6 +216,7 @@ int parse_buffer(const char *buf, size_t len, int N, int dtype, uint32_t seed, g
               k.err_code = GTK_ERR_PARSE;
               k.err_msg = "input tensors must follow base-1 indexing";
             }
+            out->idx[n][line] = 0;
           } else {
             out->idx[n][line] = v - 1;
             if (v > k.maxd[n]) k.maxd[n] = v;
@@ -164,22 +236,23 @@ int parse_buffer(const char *buf, size_t len, int N, int dtype, uint32_t seed, g
           k.err_msg = "line has fewer indices than the tensor order";
         }
       } else if (vs) {
-        vtok.assign(vs, ve);
-        char *endp = nullptr;
-        double d = strtod(vtok.c_str(), &endp);
-        if (endp == vtok.c_str()) {
-          if (line < k.err_line) {
+        double d = 0;
+        if (!parse_value_fast(vs, ve, d)) {
+          vtok.assign(vs, ve);
+          char *endp = nullptr;
+          d = strtod(vtok.c_str(), &endp);
+          if (endp == vtok.c_str() && line < k.err_line) {
             k.err_line = line;
             k.err_code = GTK_ERR_PARSE;
             k.err_msg = "value token is not a number";
           }
-        } else if (dtype == GTK_F32) {
-          out->vf[line] = (float)d;
-        } else {
-          out->vd[line] = d;
         }
+        if (dtype == GTK_F32)
+          out->vf[line] = (float)d;  // std::stod, then narrowed to value_t
+        else
+          out->vd[line] = d;
       } else {
-        missing[line] = 1;
+        k.missing.push_back(line);
       }
       ++line;
       p = nl + 1;
@@ -202,33 +275,58 @@ int parse_buffer(const char *buf, size_t len, int N, int dtype, uint32_t seed, g
     out->dims[n] = 0;
     for (auto &c : ch) out->dims[n] = std::max(out->dims[n], c.maxd[n]);
   }
-  // values of lines without one, in file order
+  // values of lines without one, in file order (chunks are in file order)
   GlibcRand g(seed);
   uint64_t draws = 0;
-  for (uint64_t l = 0; l < nnz; ++l) {
-    if (!missing[l]) continue;
-    if (dtype == GTK_F32)
-      out->vf[l] = g.frand01<float>();
-    else
-      out->vd[l] = g.frand01<double>();
-    ++draws;
-  }
+  for (const Chunk &c : ch)
+    for (uint64_t l : c.missing) {
+      if (dtype == GTK_F32)
+        out->vf[l] = g.frand01<float>();
+      else
+        out->vd[l] = g.frand01<double>();
+      ++draws;
+    }
   out->draws = draws;
   return 0;
 }
 
 int parse_file(const char *path, int N, int dtype, uint32_t seed, gtk_coo *out) {
-  FILE *f = fopen(path, "rb");
-  if (!f) return fail(GTK_ERR_IO, std::string("cannot open file \"") + path + "\" for reading");
-  std::vector<char> data;
-  if (fseek(f, 0, SEEK_END) == 0) {
-    long sz = ftell(f);
-    if (sz > 0) data.resize((size_t)sz);
-    fseek(f, 0, SEEK_SET);
+  const int fd = open(path, O_RDONLY);
+  if (fd < 0) return fail(GTK_ERR_IO, std::string("cannot open file \"") + path + "\" for reading");
+  struct stat st;
+  if (fstat(fd, &st) != 0) {
+    close(fd);
+    return fail(GTK_ERR_IO, std::string("cannot stat \"") + path + "\"");
   }
-  size_t got = data.empty() ? 0 : fread(data.data(), 1, data.size(), f);
-  fclose(f);
-  if (got != data.size()) return fail(GTK_ERR_IO, std::string("short read on \"") + path + "\"");
+  const size_t size = st.st_size > 0 ? (size_t)st.st_size : 0;
+  HostVec<char> data(size);  // uninitialised; each reader thread touches its own pages
+  // the file in slices read by all host threads at once (pread: no shared offset)
+  unsigned nt = std::thread::hardware_concurrency();
+  nt = std::max(1u, std::min<unsigned>(nt, 64));
+  nt = (unsigned)std::min<size_t>(nt, size / (8 << 20) + 1);
+  std::vector<int> ok(nt, 1);
+  auto rd = [&](unsigned c) {
+    size_t off = size / nt * c;
+    const size_t end = c + 1 == nt ? size : size / nt * (c + 1);
+    while (off < end) {
+      const ssize_t r = pread(fd, data.data() + off, end - off, (off_t)off);
+      if (r <= 0) {
+        if (r < 0 && errno == EINTR) continue;
+        ok[c] = 0;
+        return;
+      }
+      off += (size_t)r;
+    }
+  };
+  {
+    std::vector<std::thread> th;
+    for (unsigned c = 1; c < nt; ++c) th.emplace_back(rd, c);
+    rd(0);
+    for (auto &x : th) x.join();
+  }
+  close(fd);
+  for (int v : ok)
+    if (!v) return fail(GTK_ERR_IO, std::string("short read on \"") + path + "\"");
   return parse_buffer(data.data(), data.size(), N, dtype, seed, out);
 }
 

@@ -52,6 +52,54 @@ PARSE_TEXTS = [
 ]
 
 
+def _value_tokens(rng, n):
+    """Value tokens in the forms tensor files hold, and the edge cases of the
+    parser's exact decimal fast path (digit counts around 19, exponents around
+    +-22, signed zeros, forms it leaves to strtod)."""
+    toks = []
+    x = rng.random(n)
+    toks += [f"{v:.9g}" for v in x.astype(np.float32)]
+    toks += [f"{v:.17g}" for v in x[: n // 4]]
+    toks += [f"{v:.6e}" for v in rng.lognormal(0, 8, n // 4)]
+    toks += [f"{v:.15g}" for v in rng.normal(0, 1e3, n // 4)]
+    toks += [str(int(v)) for v in rng.integers(0, 10 ** 12, n // 8)]
+    toks += ["0", "-0", "+0.0", "0.000", "1", "-1", "5.", ".5", "-.25", "+7", "1e5", "1E-5", "2.5e+3",
+             "0.1e2", "123456789012345678", "1234567890123456789", "12345678901234567890",
+             "9007199254740993", "9007199254740992", "0.30000000000000004", "1e22", "1e23", "1e-22",
+             "1e-23", "4.9e-324", "1.7976931348623157e308", "1e400", "1e-400", "0x1p-3", "inf", "-nan",
+             "1.5abc", "3.14159265358979323846264338327950288", "000000000000000000000001.5",
+             "0.0000000000000000000000000001234", "7e0", "1e+0022", "123.456e-10"]
+    return toks
+
+
+@pytest.mark.parametrize("dtype", [0, 1])
+def test_parser_values_match_correct_rounding(native, dtype):
+    """Every value token reads as strtod reads it (a correctly rounded double,
+    then narrowed to value_t): against Python's float(), also correctly rounded,
+    for the tokens the fast path takes and those it leaves to strtod."""
+    rng = np.random.default_rng(11)
+    toks = _value_tokens(rng, 4000)
+    text = "".join(f"{i % 7 + 1}\t{i % 5 + 1}\t{i % 3 + 1}\t{t}\n" for i, t in enumerate(toks)).encode()
+    coo = gtk.parse_buffer(text, 3, dtype, rand_seed=1)
+    _, gv = coo.arrays()
+    want = []
+    for t in toks:
+        m = re.match(r"[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?", t)
+        if t.lower().lstrip("+-").startswith(("inf", "nan")) or t.startswith("0x"):
+            want.append(float.fromhex(t) if t.startswith("0x") else float(t))
+        else:
+            want.append(float(m.group(0)))
+    want = np.array(want, dtype=np.float64)
+    if dtype == 0:
+        with np.errstate(over="ignore"):  # 1e400 and the like narrow to inf, as in C
+            want = want.astype(np.float32)
+    got = gv
+    same = (got == want) | (np.isnan(got) & np.isnan(want))
+    assert same.all(), [(toks[i], got[i], want[i]) for i in np.flatnonzero(~same)[:10]]
+    # signs of zeros too
+    assert np.array_equal(np.signbit(got), np.signbit(want))
+
+
 @pytest.mark.parametrize("text", PARSE_TEXTS)
 @pytest.mark.parametrize("dtype", [0, 1])
 def test_parser_matches_oracle(native, text, dtype):
