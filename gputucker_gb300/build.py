@@ -30,7 +30,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # host code without FP contraction: the serial value_t sums that restate the
 # reference's (its norm) must round every product and sum separately
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off", "-I" + INCLUDE, "-I" + CSRC]
-LIB_SOURCES = ["api.cpp", "parse.cpp", "gen.cpp", "partition.cu", "sweep.cu", "tc_sweep.cu", "noalloc.cu", "batch.cu", "plan.cpp", "warmstart.cu", "tc_stream.cu", "core_update.cu", "validate.cu"]
+LIB_SOURCES = ["api.cpp", "parse.cpp", "gen.cpp", "partition.cu", "sweep.cu", "tc_sweep.cu", "noalloc.cu", "batch.cu", "plan.cpp", "warmstart.cu", "tc_stream.cu", "core_update.cu", "validate.cu", "hostpart.cpp"]
 
 
 def _nvcc() -> str:

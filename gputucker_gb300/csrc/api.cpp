@@ -187,16 +187,103 @@ int dalloc(DevTensor &t, void **p, size_t bytes) {
   return 0;
 }
 
+int need_resident(const DevTensor &t, const char *what) {
+  if (!t.streamed) return 0;
+  return fail(GTK_ERR_UNSUPPORTED, std::string(what) + " needs the device-resident layout; this handle streams its "
+                                                        "views from host memory");
+}
+
 static void release(DevTensor &t) {
   if (t.dev >= 0) cudaSetDevice(t.dev);
   if (t.stream) cudaStreamSynchronize(t.stream);
+  if (t.copy_stream) cudaStreamSynchronize(t.copy_stream);
   drop_graph(t);
   for (const auto &a : t.allocs) dev_free(t.dev, a.first, a.second);
   t.allocs.clear();
   if (t.tev0) cudaEventDestroy(t.tev0);
   if (t.tev1) cudaEventDestroy(t.tev1);
+  for (int b = 0; b < 2; ++b) {
+    if (t.stage_ready[b]) cudaEventDestroy(t.stage_ready[b]);
+    if (t.stage_free[b]) cudaEventDestroy(t.stage_free[b]);
+    t.stage_ready[b] = t.stage_free[b] = nullptr;
+  }
+  if (t.hp && t.hp->pinned) {
+    for (int m = 0; m < t.N; ++m) {
+      for (int k = 0; k < t.N; ++k)
+        if (!t.hp->vidx[m][k].empty()) cudaHostUnregister(t.hp->vidx[m][k].data());
+      if (!t.hp->vval[m].empty()) cudaHostUnregister(t.hp->vval[m].data());
+    }
+    t.hp->pinned = false;
+  }
+  if (t.copy_stream) cudaStreamDestroy(t.copy_stream);
+  t.copy_stream = nullptr;
   if (t.stream) cudaStreamDestroy(t.stream);
   t.stream = nullptr;
+}
+
+namespace {
+// device bytes of the resident layout (persistent arrays) and of the partition's
+// temporaries, to decide between the resident and the streamed layout
+void resident_bytes(const DevTensor &t, uint64_t *persist, uint64_t *temp) {
+  const uint64_t n = t.nnz, vs = t.vsize, N = (uint64_t)t.N;
+  uint64_t p = (t.nblk + 1) * 8 + n * vs * 2;  // blk_ptr, blk_val, val_in
+  for (int k = 0; k < t.N; ++k)
+    p += n * 4 * (3 + N) + n * vs + t.nblk * (uint64_t)(t.bd[k] + 1) * 8;  // blk_idx, where, vperm, views, count
+  *persist = p;
+  *temp = n * (4 * N + 4 * 8) + n * 64;  // uploaded coordinates, sort scratch, block-major copies, records
+}
+}  // namespace
+
+// The streamed layout: the partition in host memory (hostpart.cpp), page-locked
+// views where the host allows, and two device staging buffers of `chunk`
+// nonzeros (GTK_STREAM_CHUNK nonzeros, else as many as fit a quarter of the
+// memory the handle may still use, at most 2^26).
+int setup_streamed(DevTensor &t, const gtk_coo &coo) {
+  if (int rc = build_host_partition(t, coo)) return rc;
+  HostPart &h = *t.hp;
+  const uint64_t per = (uint64_t)t.N * 4 + t.vsize;  // staged bytes per nonzero
+  uint64_t chunk = 0;
+  if (const char *s = getenv("GTK_STREAM_CHUNK")) chunk = strtoull(s, nullptr, 10);
+  if (!chunk) {
+    const uint64_t cap = memory_cap();
+    size_t fr = 0, tot = 0;
+    GTK_CUDA(cudaMemGetInfo(&fr, &tot));
+    uint64_t room = (uint64_t)fr + dev_cached_bytes(t.dev);
+    if (cap) room = std::min<uint64_t>(room, cap > t.bytes ? cap - t.bytes : 0);
+    chunk = room / 4 / per;
+    chunk = std::min<uint64_t>(chunk, 1ull << 26);
+  }
+  chunk = std::max<uint64_t>(std::min<uint64_t>(chunk, t.nnz), 1);
+  t.chunk = chunk;
+  for (int b = 0; b < 2; ++b) {
+    for (int k = 0; k < t.N; ++k)
+      if (int rc = dalloc(t, (void **)&t.stage_idx[b][k], chunk * 4)) return rc;
+    if (int rc = dalloc(t, &t.stage_val[b], chunk * t.vsize)) return rc;
+    GTK_CUDA(cudaEventCreateWithFlags(&t.stage_ready[b], cudaEventDisableTiming));
+    GTK_CUDA(cudaEventCreateWithFlags(&t.stage_free[b], cudaEventDisableTiming));
+  }
+  GTK_CUDA(cudaStreamCreateWithFlags(&t.copy_stream, cudaStreamNonBlocking));
+  // page-locked views copy asynchronously; without registration (not allowed, or
+  // out of lockable memory) the copies read pageable memory
+  if (t.nnz) {
+    bool ok = true;
+    for (int m = 0; m < t.N && ok; ++m) {
+      for (int k = 0; k < t.N && ok; ++k)
+        ok = cudaHostRegister(h.vidx[m][k].data(), t.nnz * 4, cudaHostRegisterDefault) == cudaSuccess;
+      if (ok) ok = cudaHostRegister(h.vval[m].data(), t.nnz * t.vsize, cudaHostRegisterDefault) == cudaSuccess;
+      if (!ok) {
+        cudaGetLastError();
+        // undo this mode's partial registration and every earlier mode's
+        for (int mm = 0; mm <= m; ++mm) {
+          for (int k = 0; k < t.N; ++k) cudaHostUnregister(h.vidx[mm][k].data());
+          cudaHostUnregister(h.vval[mm].data());
+        }
+        cudaGetLastError();
+      }
+    }
+    h.pinned = ok;
+  }
+  return 0;
 }
 
 // slab layout [rows][J] <-> device [rows][ldf]
@@ -418,15 +505,32 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
   auto A = [&](void **p, size_t b) {
     if (!rc) rc = dalloc(*t, p, b);
   };
-  A((void **)&t->blk_ptr, (nblk + 1) * 8);
-  A(&t->blk_val, nnz * vs);
+  // the resident layout, or -- when it does not fit the memory the handle may
+  // use (GTK_DEVICE_MEMORY_CAP, else the device's free memory) -- the streamed one
+  {
+    uint64_t persist = 0, temp = 0;
+    resident_bytes(*t, &persist, &temp);
+    const uint64_t cap = memory_cap();
+    size_t fr = 0, tot = 0;
+    if ((rc = ck(cudaMemGetInfo(&fr, &tot), "cudaMemGetInfo"))) return bail(rc);
+    const uint64_t avail = (uint64_t)fr + dev_cached_bytes(device);
+    t->streamed = (cap && persist > cap) || persist + temp > avail;
+    const char *force = getenv("GTK_FORCE_STREAMED");
+    if (force && *force == '1') t->streamed = true;
+  }
+  if (!t->streamed) {
+    A((void **)&t->blk_ptr, (nblk + 1) * 8);
+    A(&t->blk_val, nnz * vs);
+  }
   for (int n = 0; n < N; ++n) {
-    A((void **)&t->blk_idx[n], nnz * 4);
-    A((void **)&t->count[n], nblk * (uint64_t)(bd[n] + 1) * 8);
-    A((void **)&t->where[n], nnz * 4);
-    A((void **)&t->vperm[n], nnz * 4);
-    A(&t->vval[n], nnz * vs);
-    for (int k = 0; k < N; ++k) A((void **)&t->vidx[n][k], nnz * 4);
+    if (!t->streamed) {
+      A((void **)&t->blk_idx[n], nnz * 4);
+      A((void **)&t->count[n], nblk * (uint64_t)(bd[n] + 1) * 8);
+      A((void **)&t->where[n], nnz * 4);
+      A((void **)&t->vperm[n], nnz * 4);
+      A(&t->vval[n], nnz * vs);
+      for (int k = 0; k < N; ++k) A((void **)&t->vidx[n][k], nnz * 4);
+    }
     A(&t->fac[n], t->rows[n] * t->ldf * vs);
     A(&t->corep[n], (core_n / rank) * t->ldf * vs);
   }
@@ -445,7 +549,11 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
   }
   if ((rc = ck(cudaMemsetAsync(t->status, 0, 16, t->stream), "memset"))) return bail(rc);
   if ((rc = ck(cudaMemsetAsync(t->nfallback, 0, 16, t->stream), "memset"))) return bail(rc);
-  rc = build_partition(*t, *coo);
+  if (t->streamed) {
+    if ((rc = setup_streamed(*t, *coo))) return bail(rc);
+  } else {
+    rc = build_partition(*t, *coo);
+  }
   if (rc) return bail(rc);
   *out = t;
   return 0;
@@ -468,6 +576,8 @@ int gtk_tensor_info_get(const gtk_tensor *t, gtk_tensor_info *info) {
   }
   info->norm = t->norm;
   info->device_bytes = t->bytes;
+  info->streamed = t->streamed ? 1 : 0;
+  info->stream_chunk = t->chunk;
   return 0;
 }
 
@@ -490,6 +600,13 @@ int gtk_block_data(const gtk_tensor *t, uint64_t b, uint32_t *const *idx, void *
   if (b >= t->nblk) return fail(GTK_ERR_ARG, "block id out of range");
   if (int rc = set_dev(t)) return rc;
   const uint64_t s = t->h_blk_ptr[b], n = t->h_blk_ptr[b + 1] - s;
+  if (t->streamed) {
+    if (idx)
+      for (int k = 0; k < t->N; ++k)
+        if (idx[k] && n) memcpy(idx[k], t->hp->blk_idx[k].data() + s, n * 4);
+    if (values && n) memcpy(values, t->hp->blk_val.data() + s * t->vsize, n * t->vsize);
+    return 0;
+  }
   if (idx)
     for (int k = 0; k < t->N; ++k)
       if (idx[k] && n) GTK_CUDA(cudaMemcpyAsync(idx[k], t->blk_idx[k] + s, n * 4, cudaMemcpyDeviceToHost, t->stream));
@@ -506,6 +623,11 @@ int gtk_block_segments(const gtk_tensor *t, uint64_t b, int mode, uint64_t *coun
   if (int rc = set_dev(t)) return rc;
   const uint64_t s = t->h_blk_ptr[b], n = t->h_blk_ptr[b + 1] - s;
   const uint64_t rows = (uint64_t)t->bd[mode] + 1;
+  if (t->streamed) {
+    if (count_nnz) memcpy(count_nnz, t->hp->count[mode].data() + b * rows, rows * 8);
+    if (where_nnz && n) memcpy(where_nnz, t->hp->where[mode].data() + s, n * 4);
+    return 0;
+  }
   if (count_nnz)
     GTK_CUDA(cudaMemcpyAsync(count_nnz, t->count[mode] + b * rows, rows * 8, cudaMemcpyDeviceToHost, t->stream));
   if (where_nnz && n)
@@ -625,6 +747,7 @@ int gtk_update_mode(gtk_tensor *t, int mode) {
 
 int gtk_validate(gtk_tensor *t, uint64_t *violations) {
   if (!t || !violations) return fail(GTK_ERR_ARG, "null argument");
+  if (int rc = need_resident(*t, "gtk_validate")) return rc;
   if (int rc = set_dev(t)) return rc;
   GTK_GUARD_BEGIN
   return run_validate(*t, violations);
@@ -633,6 +756,7 @@ int gtk_validate(gtk_tensor *t, uint64_t *violations) {
 
 int gtk_update_core(gtk_tensor *t, int cg_iters, int *iters_run, double *rel_residual) {
   if (int rc = ready(t)) return rc;
+  if (int rc = need_resident(*t, "gtk_update_core")) return rc;
   if (cg_iters < 0) return fail(GTK_ERR_ARG, "negative iteration count");
   GTK_GUARD_BEGIN
   return run_update_core(*t, cg_iters, iters_run, rel_residual);
@@ -698,6 +822,7 @@ int gtk_tucker_decomposition(gtk_tensor *t, int max_iters, double tol, double *f
 
 int gtk_compute_delta(gtk_tensor *t, int mode, void *delta) {
   if (int rc = ready(t)) return rc;
+  if (int rc = need_resident(*t, "gtk_compute_delta")) return rc;
   if (mode < 0 || mode >= t->N || !delta) return fail(GTK_ERR_ARG, "bad mode or null output");
   GTK_GUARD_BEGIN
   const size_t bytes = t->nnz * (size_t)t->J * t->vsize;

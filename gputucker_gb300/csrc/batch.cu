@@ -171,8 +171,10 @@ int gtk_set_kernel_variant(gtk_tensor *t, int variant) {
   if (variant < GTK_VARIANT_AUTO || variant > GTK_VARIANT_REFERENCE_ORDER) return fail(GTK_ERR_ARG, "unknown variant");
   if (variant == GTK_VARIANT_TENSOR_CORE && t->precision == GTK_PREC_PLAIN)
     return fail(GTK_ERR_UNSUPPORTED, "the tensor-core variant needs a precision form (gtk_set_precision)");
-  if (variant == GTK_VARIANT_REFERENCE_ORDER)
+  if (variant == GTK_VARIANT_REFERENCE_ORDER) {
+    if (int rc = need_resident(*t, "the reference-order variant")) return rc;
     if (int rc = ensure_norm_ref(*t)) return rc;
+  }
   t->variant = variant;
   fit_invalidate(*t);
   drop_graph(*t);
@@ -257,6 +259,7 @@ int gtk_batch_create(gtk_tensor *const *tensors, int count, gtk_batch **out) {
   for (int i = 0; i < count; ++i) {
     if (!tensors[i] || tensors[i]->dev != tensors[0]->dev)
       return fail(GTK_ERR_ARG, "every tensor of a batch must exist and share one device");
+    if (int rc = need_resident(*tensors[i], "a batch")) return rc;
     for (int k = 0; k < i; ++k)
       if (tensors[k] == tensors[i]) return fail(GTK_ERR_ARG, "a tensor appears twice in the batch");
   }

@@ -118,6 +118,28 @@ struct gtk_coo {
 
 namespace gtk {
 
+// A contiguous range of a mode view that the mode kernels read in place of the
+// resident view (the streamed layout's staging buffers)
+struct ViewRange {
+  const uint32_t *coord[kMaxOrder];
+  const void *val;
+  uint64_t nnz;
+};
+
+// The blocked arrays and mode views in host memory (the streamed layout), with
+// the same definitions and layouts as the device arrays of DevTensor below;
+// vval/blk_val hold value_t bytes.
+struct HostPart {
+  HostVec<uint64_t> blk_ptr;
+  HostVec<uint32_t> blk_idx[kMaxOrder];
+  HostVec<unsigned char> blk_val;
+  HostVec<uint64_t> count[kMaxOrder];
+  HostVec<uint32_t> where[kMaxOrder];
+  HostVec<uint32_t> vidx[kMaxOrder][kMaxOrder];
+  HostVec<unsigned char> vval[kMaxOrder];
+  bool pinned = false;  // vidx/vval page-locked (cudaHostRegister)
+};
+
 // Device buffers of one resident tensor.  Layout in HBM:
 //   blocked arrays (block-major, the reference's Block order):
 //     blk_ptr[nblk+1] u64, blk_idx[n][nnz] u32 local coords, blk_val[nnz] V,
@@ -193,7 +215,33 @@ struct DevTensor {
 
   std::vector<std::pair<void *, size_t>> allocs;  // device blocks of the handle and their sizes
   uint64_t bytes = 0;
+
+  // Streamed layout, for tensors whose resident layout does not fit the device
+  // memory the handle may use: the blocked arrays and the mode views stay in host
+  // memory (hp), and every pass over a mode view streams it through two device
+  // staging buffers of `chunk` nonzeros -- copies on copy_stream, kernels on
+  // stream, events hand each buffer back and forth.  Factors, core, Gram/RHS and
+  // the fit's partial sums stay resident.
+  bool streamed = false;
+  std::unique_ptr<HostPart> hp;
+  uint64_t chunk = 0;
+  uint32_t *stage_idx[2][kMaxOrder] = {};
+  void *stage_val[2] = {};
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t stage_ready[2] = {}, stage_free[2] = {};
+  double stream_copy_bytes = 0;  // host-to-device bytes the streamed passes moved
+  const ViewRange *range = nullptr;  // set around a launch: the kernels read this range, not the resident view
 };
+
+// the view a mode kernel reads: the resident view of `mode`, or t.range
+inline ViewRange view_of(const DevTensor &t, int mode) {
+  if (t.range) return *t.range;
+  ViewRange r;
+  for (int k = 0; k < kMaxOrder; ++k) r.coord[k] = t.vidx[mode][k];
+  r.val = t.vval[mode];
+  r.nnz = t.nnz;
+  return r;
+}
 
 // device memory helpers (api.cpp)
 int dalloc(DevTensor &t, void **p, size_t bytes);
@@ -228,6 +276,10 @@ struct DevBuf {
 
 // partition.cu
 int build_partition(DevTensor &t, const gtk_coo &coo);
+// hostpart.cpp: the blocked arrays and mode views of the streamed layout, in t.hp
+int build_host_partition(DevTensor &t, const gtk_coo &coo);
+// GTK_ERR_UNSUPPORTED for a streamed handle: `what` needs the resident views
+int need_resident(const DevTensor &t, const char *what);
 
 // sweep.cu
 int upload_core_perms(DevTensor &t, const void *core_host);

@@ -877,11 +877,12 @@ __global__ void k_fit_gram(const double *__restrict__ gram, const V *__restrict_
   if (threadIdx.x == 0) partial[blockIdx.x] = (blockIdx.x == 0 ? normsq : 0.0) - tot;
 }
 
-__global__ void k_sum_fit(const double *__restrict__ partial, int m, double *__restrict__ out) {
+// out = the sum of partial[0, m) (acc: out += it, the streamed passes' chunks)
+__global__ void k_sum_fit(const double *__restrict__ partial, int m, double *__restrict__ out, int acc = 0) {
   if (threadIdx.x == 0 && blockIdx.x == 0) {
     double s = 0;
     for (int i = 0; i < m; ++i) s += partial[i];
-    *out = s;
+    *out = acc ? *out + s : s;
   }
 }
 
@@ -980,17 +981,18 @@ int prepare_fn(const void *fn, size_t smem) {
 ModeArgs make_args(const DevTensor &t, int mode) {
   ModeArgs a;
   memset(&a, 0, sizeof(a));
+  const ViewRange vr = view_of(t, mode);
   for (int k = 0; k < t.N; ++k) {
-    a.coord[k] = t.vidx[mode][k];
+    a.coord[k] = vr.coord[k];
     a.fac[k] = t.fac[k];
   }
-  a.val = t.vval[mode];
+  a.val = vr.val;
   a.corep = t.corep[mode];
   a.vperm = t.vperm[mode];
   a.gram = t.gram;
   a.partial = t.partial;
   a.status = t.status;
-  a.nnz = t.nnz;
+  a.nnz = vr.nnz;
   a.N = t.N;
   a.J = t.J;
   a.ldf = t.ldf;
@@ -1063,7 +1065,7 @@ template <class V, int KIND> static int launch_mode(DevTensor &t, int mode, void
   int per_sm = 0;
   GTK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, kThreads, L.smem));
   if (per_sm < 1) return fail(GTK_ERR_UNSUPPORTED, "mode kernel does not fit on an SM");
-  const uint64_t ntiles = (t.nnz + L.tn - 1) / L.tn;
+  const uint64_t ntiles = (a.nnz + L.tn - 1) / L.tn;
   uint64_t grid = std::min<uint64_t>(ntiles, (uint64_t)per_sm * t.num_sms);
   if (KIND == kFit) grid = std::min<uint64_t>(grid, kFitGridMax);
   if (grid < 1) grid = 1;
@@ -1103,6 +1105,39 @@ void fit_after_sweep(DevTensor &t) {
   t.fit_from_store = !t.fit_from_gram && t.dstore != nullptr;
 }
 
+// One pass of a mode kernel over the streamed view of `mode` (the streamed
+// layout): chunk c goes to staging buffer c % 2 on copy_stream -- after the
+// kernel that read that buffer last has finished -- while the kernel of chunk
+// c - 1 runs on the handle's stream; `launch` enqueues the kernel for t.range.
+template <class F> static int stream_pass(DevTensor &t, int mode, F launch) {
+  const HostPart &h = *t.hp;
+  uint64_t c = 0;
+  for (uint64_t c0 = 0; c0 < t.nnz; c0 += t.chunk, ++c) {
+    const int b = (int)(c & 1);
+    const uint64_t m = std::min<uint64_t>(t.chunk, t.nnz - c0);
+    GTK_CUDA(cudaStreamWaitEvent(t.copy_stream, t.stage_free[b], 0));
+    for (int k = 0; k < t.N; ++k)
+      GTK_CUDA(cudaMemcpyAsync(t.stage_idx[b][k], h.vidx[mode][k].data() + c0, m * 4, cudaMemcpyHostToDevice,
+                               t.copy_stream));
+    GTK_CUDA(cudaMemcpyAsync(t.stage_val[b], h.vval[mode].data() + c0 * t.vsize, m * t.vsize, cudaMemcpyHostToDevice,
+                             t.copy_stream));
+    GTK_CUDA(cudaEventRecord(t.stage_ready[b], t.copy_stream));
+    GTK_CUDA(cudaStreamWaitEvent(t.stream, t.stage_ready[b], 0));
+    ViewRange r;
+    for (int k = 0; k < kMaxOrder; ++k) r.coord[k] = k < t.N ? t.stage_idx[b][k] : nullptr;
+    r.val = t.stage_val[b];
+    r.nnz = m;
+    t.range = &r;
+    const int rc = launch();
+    t.range = nullptr;
+    if (rc) return rc;
+    GTK_CUDA(cudaEventRecord(t.stage_free[b], t.stream));
+    t.stream_copy_bytes += (double)m * (double)(t.N * 4 + t.vsize);
+    t.launches += 1;
+  }
+  return 0;
+}
+
 template <class V> static int update_impl(DevTensor &t, int mode) {
   static const char *const kNames[kMaxOrder] = {"mode update 0", "mode update 1", "mode update 2", "mode update 3",
                                                  "mode update 4", "mode update 5", "mode update 6", "mode update 7"};
@@ -1115,7 +1150,7 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   // Gram/RHS (k_fit_gram), otherwise from delta, which the pass then stores (the
   // reference-order variant stores it on every mode: its B and C come from it)
   void *dstore = nullptr;
-  if (((last && !tc) || t.variant == kVarRefOrder) && t.nnz) {
+  if (!t.streamed && ((last && !tc) || t.variant == kVarRefOrder) && t.nnz) {
     if (int rc = ensure_dstore(t)) return rc;
     dstore = t.dstore;
   }
@@ -1123,7 +1158,12 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
   cudaEvent_t ev = nullptr;
   if (int rc = prof_begin(t, &ev)) return rc;
   GTK_CUDA(cudaMemsetAsync(t.gram, 0, t.rows[mode] * (uint64_t)E * 8, t.stream));
-  if (t.nnz) {
+  if (t.nnz && t.streamed) {
+    if (int rc = stream_pass(t, mode, [&]() {
+          return tc ? run_mode_tc(t, mode, 0, nullptr, nullptr) : launch_mode<V, kUpdate>(t, mode, nullptr, nullptr);
+        }))
+      return rc;
+  } else if (t.nnz) {
     if (tc) {
       if (int rc = run_mode_tc(t, mode, 0, dstore, nullptr)) return rc;
     } else if (int rc = launch_mode<V, kUpdate>(t, mode, dstore, nullptr)) {
@@ -1198,7 +1238,8 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
     t.launches += 1;
   }
   t.fit_from_store = dstore != nullptr && last;
-  t.fit_from_gram = tc && last;
+  // the streamed layout keeps no delta: every form takes the fit from the Gram/RHS
+  t.fit_from_gram = (tc || t.streamed) && last;
   if (int rc = prof_end(t, 1, ev)) return rc;
   return 0;
 }
@@ -1238,6 +1279,22 @@ template <class V> static int fit_enqueue(DevTensor &t) {
                                                 (const V *)t.fac[t.N - 1], t.nnz, t.J, t.ldf, t.partial);
     GTK_CUDA(cudaGetLastError());
     t.launches += 1;
+  } else if (t.nnz && t.streamed) {
+    // the direct fit over the streamed view, each chunk's partials added to the sum
+    GTK_CUDA(cudaMemsetAsync(t.partial + kFitGridMax, 0, 8, t.stream));
+    if (int rc = stream_pass(t, t.N - 1, [&]() -> int {
+          int g = 1;
+          if (t.precision != GTK_PREC_PLAIN) {
+            if (int rc2 = run_mode_tc(t, t.N - 1, 1, nullptr, &g)) return rc2;
+          } else if (int rc2 = launch_mode<V, kFit>(t, t.N - 1, nullptr, &g)) {
+            return rc2;
+          }
+          k_sum_fit<<<1, 32, 0, t.stream>>>(t.partial, g, t.partial + kFitGridMax, 1);
+          t.launches += 1;
+          return ck(cudaGetLastError(), "k_sum_fit");
+        }))
+      return rc;
+    return 0;
   } else if (t.nnz) {
     t.launches += 1;
     if (t.precision != GTK_PREC_PLAIN) {
@@ -1301,7 +1358,7 @@ void drop_graph(DevTensor &t) {
 // read of the error sum stays outside.
 int run_sweep(DevTensor &t, double *fit) {
   NvtxRange nvtx("sweep");
-  if (!t.use_graph) {
+  if (!t.use_graph || t.streamed) {  // streamed passes copy from the host: not captured
     for (int n = 0; n < t.N; ++n)
       if (int rc = run_update_mode(t, n)) return rc;
     return run_fit(t, fit);
@@ -1406,6 +1463,15 @@ __global__ void k_max_u32(const uint32_t *__restrict__ a, uint64_t n, uint32_t *
 int run_row_stats(DevTensor &t, int mode, uint32_t *max_count) {
   *max_count = 0;
   if (!t.nnz) return 0;
+  if (t.streamed) {  // the host view is sorted by row: the longest run
+    const HostVec<uint32_t> &r = t.hp->vidx[mode][mode];
+    uint32_t run = 0;
+    for (uint64_t i = 0; i < t.nnz; ++i) {
+      run = (i && r[i] == r[i - 1]) ? run + 1 : 1;
+      *max_count = std::max(*max_count, run);
+    }
+    return 0;
+  }
   uint32_t *cnt = nullptr;
   GTK_CUDA(malloc_retry(&cnt, (t.rows[mode] + 1) * 4));
   int rc = ck(cudaMemsetAsync(cnt, 0, (t.rows[mode] + 1) * 4, t.stream), "memset");

@@ -464,11 +464,12 @@ int run_mode_tcs(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   if (int rc = ts_prepare(L, t.num_sms, &cap, &smem)) return rc;
   ModeArgs a;
   memset(&a, 0, sizeof(a));
+  const ViewRange vr = view_of(t, mode);
   for (int k = 0; k < t.N; ++k) {
-    a.coord[k] = t.vidx[mode][k];
+    a.coord[k] = vr.coord[k];
     a.fac[k] = t.fac[k];
   }
-  a.val = t.vval[mode];
+  a.val = vr.val;
   a.corep = t.corep[mode];
   a.vperm = t.vperm[mode];
   if (kind == 0)
@@ -478,7 +479,7 @@ int run_mode_tcs(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   a.gram = t.gram;
   a.partial = t.partial;
   a.status = t.status;
-  a.nnz = t.nnz;
+  a.nnz = vr.nnz;
   a.N = t.N;
   a.J = t.J;
   a.ldf = t.ldf;
@@ -488,7 +489,7 @@ int run_mode_tcs(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   int m = 0;
   for (int k = 0; k < t.N; ++k)
     if (k != mode) a.others[m++] = k;
-  const uint64_t ntiles = (t.nnz + kTsThreads - 1) / kTsThreads;
+  const uint64_t ntiles = (a.nnz + kTsThreads - 1) / kTsThreads;
   uint64_t grid = std::min<uint64_t>(ntiles, (uint64_t)cap);
   if (kind == 1) grid = std::min<uint64_t>(grid, kTsFitGrid);
   if (grid < 1) grid = 1;

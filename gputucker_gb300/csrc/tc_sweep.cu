@@ -445,11 +445,12 @@ int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   if (int rc = tc_prepare(L, t.num_sms, &cap, &smem)) return rc;
   ModeArgs a;
   memset(&a, 0, sizeof(a));
+  const ViewRange vr = view_of(t, mode);
   for (int k = 0; k < t.N; ++k) {
-    a.coord[k] = t.vidx[mode][k];
+    a.coord[k] = vr.coord[k];
     a.fac[k] = t.fac[k];
   }
-  a.val = t.vval[mode];
+  a.val = vr.val;
   a.corep = t.corep[mode];
   a.vperm = t.vperm[mode];
   if (kind == 0)
@@ -459,7 +460,7 @@ int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   a.gram = t.gram;
   a.partial = t.partial;
   a.status = t.status;
-  a.nnz = t.nnz;
+  a.nnz = vr.nnz;
   a.N = t.N;
   a.J = t.J;
   a.ldf = t.ldf;
@@ -469,7 +470,7 @@ int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   int m = 0;
   for (int k = 0; k < t.N; ++k)
     if (k != mode) a.others[m++] = k;
-  const uint64_t ntiles = (t.nnz + kTcThreads - 1) / kTcThreads;
+  const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
   uint64_t grid = std::min<uint64_t>(ntiles, (uint64_t)cap);
   if (kind == 1) grid = std::min<uint64_t>(grid, kTcFitGrid);
   if (grid < 1) grid = 1;

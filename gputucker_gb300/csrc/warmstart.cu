@@ -668,6 +668,7 @@ int gtk_ws_set_params(gtk_ws *m, const float *params, const float *feat_mean, co
 
 int gtk_ws_features(gtk_tensor *t, int mode, float *out) {
   if (!t || !out || mode < 0 || mode >= t->N) return fail(GTK_ERR_ARG, "bad argument");
+  if (int rc = need_resident(*t, "the warm start")) return rc;
   if (t->N < 2) return fail(GTK_ERR_UNSUPPORTED, "warm start needs order >= 2");
   GTK_CUDA(cudaSetDevice(t->dev));
   const int F = ws_nfeat(t->N);
@@ -681,6 +682,7 @@ int gtk_ws_features(gtk_tensor *t, int mode, float *out) {
 
 int gtk_ws_add_example(gtk_ws *m, gtk_tensor *t) {
   if (!m || !t) return fail(GTK_ERR_ARG, "null argument");
+  if (int rc = need_resident(*t, "the warm start")) return rc;
   if (t->N != m->N || t->J != m->J) return fail(GTK_ERR_ARG, "model and tensor differ in order or rank");
   if (!t->have_factors) return fail(GTK_ERR_STATE, "the tensor has no factors to learn from");
   if (t->dev != m->dev) return fail(GTK_ERR_ARG, "model and tensor on different devices");
@@ -816,6 +818,7 @@ int gtk_ws_train(gtk_ws *m, int steps, int batch, float lr, double *final_loss) 
 
 int gtk_ws_apply(gtk_ws *m, gtk_tensor *t) {
   if (!m || !t) return fail(GTK_ERR_ARG, "null argument");
+  if (int rc = need_resident(*t, "the warm start")) return rc;
   if (t->N != m->N || t->J != m->J) return fail(GTK_ERR_ARG, "model and tensor differ in order or rank");
   if (t->dev != m->dev) return fail(GTK_ERR_ARG, "model and tensor on different devices");
   if (!t->have_core) return fail(GTK_ERR_STATE, "initialise the core first (gtk_init_random or gtk_set_core)");

@@ -150,6 +150,8 @@ class Info:
     block_dims: list
     norm: float
     device_bytes: int
+    streamed: bool = False
+    stream_chunk: int = 0
 
 
 class BlockedTensor:
@@ -173,7 +175,8 @@ class BlockedTensor:
         call("gtk_tensor_info_get", self._h, C.byref(ti))
         n = ti.order
         return Info(ti.order, ti.rank, ti.dtype, ti.device, ti.nnz, ti.block_count, list(ti.dims[:n]),
-                    list(ti.partition_dims[:n]), list(ti.block_dims[:n]), ti.norm, ti.device_bytes)
+                    list(ti.partition_dims[:n]), list(ti.block_dims[:n]), ti.norm, ti.device_bytes,
+                    bool(ti.streamed), ti.stream_chunk)
 
     # ---- partition readback (bit-exact with the reference's blocks)
     def block(self, b: int):

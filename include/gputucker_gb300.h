@@ -75,6 +75,8 @@ typedef struct gtk_tensor_info {
   uint32_t block_dims[GTK_MAX_ORDER]; /* ceil(dims/P_n) */
   double norm;                        /* ||X||, summed in FP64 (the reference sums in value_t) */
   uint64_t device_bytes;              /* HBM held by the handle */
+  uint32_t streamed;                  /* 1: the streamed layout (views in host memory, see gtk_create_blocks) */
+  uint64_t stream_chunk;              /* nonzeros per device staging buffer of the streamed layout */
 } gtk_tensor_info;
 
 /* ---- errors / version ------------------------------------------------- */
@@ -113,6 +115,23 @@ void gtk_coo_free(gtk_coo *coo);
  * device: CUDA ordinal.  rank: J, 1..GTK_MAX_RANK. */
 int gtk_create_blocks(const gtk_coo *coo, const uint32_t *partition_dims, int rank, int device, gtk_tensor **out);
 int gtk_tensor_info_get(const gtk_tensor *t, gtk_tensor_info *info);
+/* Layouts.  The resident layout keeps the blocked arrays, count_nnz/where_nnz
+ * and one row-sorted view per mode in HBM (about (N+1)(N+3)*4 + 3*value bytes
+ * per nonzero).  When that does not fit the device memory the handle may use
+ * (GTK_DEVICE_MEMORY_CAP bytes if set, else the device's free memory), or when
+ * GTK_FORCE_STREAMED=1, gtk_create_blocks builds the streamed layout instead --
+ * the reference's host<->device block pipeline for tensors beyond HBM
+ * (delta.cuh:141-213, reconstruction.cuh:132-202): the partition and the views
+ * are built in host memory (page-locked where the host allows) and every mode
+ * update streams its view through two device staging buffers of
+ * GTK_STREAM_CHUNK nonzeros (default: a quarter of the memory left, at most
+ * 2^26), copies overlapping the fused kernels on a second stream.  Factors,
+ * core and Gram/RHS stay resident; the fit comes from the last mode's Gram/RHS.
+ * Results equal the resident layout's up to the order of FP64 atomic adds.  Not
+ * available on a streamed handle (GTK_ERR_UNSUPPORTED): the reference-order
+ * variant, gtk_compute_delta, gtk_update_core, gtk_validate, the warm start,
+ * batches; gtk_set_graph is accepted but sweeps run eagerly. */
+
 /* block coordinate (N values) and nnz of one block */
 int gtk_block_info(const gtk_tensor *t, uint64_t block_id, uint32_t *coord, uint64_t *nnz);
 /* block-local coords (idx[n] -> nnz of the block) and values of one block, in the block's order */

@@ -1,0 +1,129 @@
+"""The streamed layout: tensors whose resident layout exceeds the device memory
+the handle may use keep their partition and mode views in host memory and stream
+each view through two device staging buffers per mode update (the reference's
+host<->device block pipeline, delta.cuh:141-213, reconstruction.cuh:132-202).
+
+Forced here with GTK_DEVICE_MEMORY_CAP on small tensors, the staging buffers
+made small with GTK_STREAM_CHUNK so that every pass runs over several chunks and
+rows cross chunk boundaries.  Checked: the partition bit-exact against the
+oracle, sweeps against the resident layout and the FP64 oracle (factors 1e-9,
+fit 1e-9 in FP64; the tensor-core form against its resident run), the entry
+points that need resident views refused.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+import gputucker_gb300 as gtk
+from gputucker_gb300 import _native as nat
+from oracle_util import Oracle, random_coo, rel_fro
+from test_gpu_parity import check_partition
+
+pytestmark = pytest.mark.gpu
+
+
+class _env:
+    def __init__(self, **kv):
+        self.kv = kv
+
+    def __enter__(self):
+        self.old = {k: os.environ.get(k) for k in self.kv}
+        os.environ.update({k: str(v) for k, v in self.kv.items()})
+
+    def __exit__(self, *exc):
+        for k, v in self.old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+def _case(dtype, seed=3, dims=(300, 250, 280, 260), nnz=200_000, zipf=1.1):
+    rng = np.random.default_rng(seed)
+    idx = random_coo(rng, list(dims), nnz, distinct=True, zipf=zipf)
+    vals = rng.random(len(idx[0])).astype(np.float64 if dtype == 1 else np.float32)
+    return list(dims), idx, vals
+
+
+def _streamed(coo, P, J, chunk=17_000):
+    with _env(GTK_DEVICE_MEMORY_CAP=48 << 20, GTK_STREAM_CHUNK=chunk):
+        t = gtk.create_tensor_blocks(coo, P, J)
+    assert t.info.streamed and t.info.stream_chunk == chunk, t.info
+    return t
+
+
+def test_streamed_partition_bit_exact():
+    dims, idx, vals = _case(1)
+    P = [2, 3, 2, 2]
+    coo = gtk.coo_from_arrays(idx, vals, dims=dims)
+    with _streamed(coo, P, 10) as t:
+        ora = Oracle(1, idx, vals, dims, P, 10)
+        check_partition(t, ora)
+
+
+@pytest.mark.parametrize("P", [[1, 1, 1, 1], [2, 3, 2, 2]], ids=["P1", "P2322"])
+def test_streamed_fp64_sweeps_match_resident_and_oracle(P):
+    dims, idx, vals = _case(1)
+    J = 10
+    coo = gtk.coo_from_arrays(idx, vals, dims=dims)
+    ora = Oracle(1, idx, vals, dims, P, J)
+    ora.init_random(1, 0)
+    with gtk.create_tensor_blocks(coo, P, J) as r, _streamed(coo, P, J) as s:
+        assert not r.info.streamed
+        assert s.info.device_bytes < r.info.device_bytes / 4
+        r.init_random(1, 0)
+        s.init_random(1, 0)
+        for sweep in range(3):
+            fr = r.sweep()
+            fs = s.sweep()
+            fo = ora.sweep()["fit64"]
+            for n in range(4):
+                assert rel_fro(s.get_factor(n), r.get_factor(n)) <= 1e-9, (sweep, n)
+                assert rel_fro(s.get_factor(n), ora.get_factor(n)) <= 1e-9, (sweep, n)
+            assert abs(fs - fr) <= 1e-9 and abs(fs - fo) <= 1e-9, (sweep, fs, fr, fo)
+        # the direct fit over the streamed view (after new factors: no Gram to use)
+        for n in range(4):
+            s.set_factor(n, s.get_factor(n))
+        assert abs(s.reconstruction() - fo) <= 1e-9
+
+
+def test_streamed_tensor_core_form_matches_resident():
+    dims, idx, vals = _case(0, seed=4)
+    P, J = [1, 2, 1, 2], 10
+    coo = gtk.coo_from_arrays(idx, vals, dims=dims)
+    with gtk.create_tensor_blocks(coo, P, J) as r, _streamed(coo, P, J, chunk=23_000) as s:
+        for t in (r, s):
+            t.init_random(1, 0)
+            t.set_precision("bf16")
+        for sweep in range(3):
+            fr, fs = r.sweep(), s.sweep()
+            assert abs(fs - fr) <= 1e-5, (sweep, fs, fr)
+        for n in range(4):
+            assert rel_fro(s.get_factor(n), r.get_factor(n)) <= 1e-4, n
+        # plain FP32 through the streamed layout: its fit from the Gram/RHS
+        for t in (r, s):
+            t.init_random(1, 0)
+            t.set_precision("plain")
+        for sweep in range(2):
+            fr, fs = r.sweep(), s.sweep()
+            assert abs(fs - fr) <= 1e-5, (sweep, fs, fr)
+
+
+def test_streamed_refuses_resident_only_calls():
+    dims, idx, vals = _case(1, nnz=20_000)
+    coo = gtk.coo_from_arrays(idx, vals, dims=dims)
+    lib = nat.load()
+    with _streamed(coo, [1, 1, 1, 1], 4, chunk=5_000) as t:
+        t.init_random(1, 0)
+        with pytest.raises(gtk.GTKError):
+            t.compute_delta(0)
+        with pytest.raises(gtk.GTKError):
+            t.set_kernel_variant("reference_order")
+        v = np.zeros(16, np.uint64)
+        rc = lib.gtk_validate(t.handle, v.ctypes.data_as(nat.U64P))
+        assert rc == nat.GTK_ERR_UNSUPPORTED
+        t.set_graph(True)  # accepted; the sweep runs eagerly
+        f1 = t.sweep()
+        assert 0.0 < f1 <= 1.0
