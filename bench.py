@@ -86,6 +86,10 @@ def args_parse():
     p.add_argument("--cpu-sample", type=int, default=200_000,
                    help="nonzeros of the CPU legs' sample (the cpu_baseline and the reference arm time the same one)")
     p.add_argument("--no-text", action="store_true", help="skip the end-to-end job from the text format")
+    p.add_argument("--no-e2e-compare", action="store_true",
+                   help="skip the end-to-end jobs that upload the COO by cudaMemcpy (GTK_HOST_DIRECT=0)")
+    p.add_argument("--e2e-pageable", action="store_true",
+                   help="also run the end-to-end jobs from pageable (not page-locked) host arrays")
     p.add_argument("--precision", choices=["plain", "bf16", "tf32"], default="bf16",
                    help="tensor-core form timed beside plain FP32 (plain: only the plain form)")
     p.add_argument("--workload", choices=["zipf4d_100M", "batch256", "warmstart", "precision3d"],
@@ -819,9 +823,10 @@ def run_e2e(args, cfg, coo, form, nnz, device, dist):
         t3 = time.perf_counter()
         facs = [tt.get_factor(n) for n in range(N)]
         t4 = time.perf_counter()
-        ph = {"create_s": t1 - t0, "create_upload_ms": tt.profile_read(5)[0],
+        ph = {"create_s": t1 - t0, "create_read_ms": tt.profile_read(5)[0],
               "create_partition_kernels_ms": tt.profile_read(6)[0], "init_s": t2 - t1,
-              "sweeps_s": t3 - t2, "readback_s": t4 - t3, "job_s": t4 - t0}
+              "sweeps_s": t3 - t2, "readback_s": t4 - t3, "job_s": t4 - t0,
+              "host_direct": int(tt.info.host_direct)}
         tt.close()
         return ph, sum(f.nbytes for f in facs)
 
@@ -830,6 +835,23 @@ def run_e2e(args, cfg, coo, form, nnz, device, dist):
     for _ in range(max(1, args.e2e_runs)):
         ph, fbytes = job(coo)
         jobs.append(ph)
+    # the same jobs with the COO uploaded by cudaMemcpy before the partition
+    # (GTK_HOST_DIRECT=0) instead of read in place by its first kernel
+    upload = []
+    if not args.no_e2e_compare:
+        os.environ["GTK_HOST_DIRECT"] = "0"
+        try:
+            upload = [job(coo)[0] for _ in range(max(1, args.e2e_runs))]
+        finally:
+            os.environ.pop("GTK_HOST_DIRECT", None)
+    # the same jobs from pageable (not page-locked) copies of the host arrays
+    pageable = None
+    if args.e2e_pageable:
+        idx, vals = coo.arrays()
+        unpinned = gtk.coo_from_arrays(idx, vals, dims=coo.dims)
+        del idx, vals
+        pageable = [job(unpinned)[0] for _ in range(max(1, args.e2e_runs))]
+        unpinned.free()
     walls = [j["job_s"] for j in jobs]
     med = dist.max(statistics.median(walls))
     best = dist.max(min(walls))
@@ -837,11 +859,24 @@ def run_e2e(args, cfg, coo, form, nnz, device, dist):
     out = {
         "value": dist.world * N * nnz * sweeps / med, "unit": "nnz/s",
         "h2d_bytes_per_step": int(h2d + fbytes + 4 * J ** N), "d2h_bytes_per_step": int(fbytes + 8 * sweeps),
-        "step": f"create_blocks from pinned host COO + init + {sweeps} sweeps with fit ({form}) + factor readback",
+        "step": f"create_blocks from the page-locked host COO (read in place by the partition's first kernel "
+                f"where the device reaches host memory, else uploaded) + init + {sweeps} sweeps with fit ({form}) "
+                f"+ factor readback",
         "statistic": f"median of {len(walls)} jobs (the first job also maps the device memory the later ones reuse)",
         "wall_s": med, "fastest_job_s": best, "fastest_job_value": dist.world * N * nnz * sweeps / best,
         "jobs": [{k: round(v, 5) for k, v in j.items()} for j in jobs],
     }
+    if upload:
+        uw = statistics.median([j["job_s"] for j in upload])
+        out["upload_copy"] = {"value": dist.world * N * nnz * sweeps / uw, "wall_s": uw,
+                              "jobs": [{k: round(v, 5) for k, v in j.items()} for j in upload],
+                              "step": "the same jobs with the COO uploaded by cudaMemcpyAsync first "
+                                      "(GTK_HOST_DIRECT=0)"}
+    if pageable:
+        pw = statistics.median([j["job_s"] for j in pageable])
+        out["pageable"] = {"value": dist.world * N * nnz * sweeps / pw, "wall_s": pw,
+                           "jobs": [{k: round(v, 5) for k, v in j.items()} for j in pageable],
+                           "step": "the same jobs from pageable copies of the host arrays"}
     if not args.no_text:
         import tempfile
         d = tempfile.mkdtemp(prefix="gtk_bench_")

@@ -59,7 +59,7 @@ class TensorInfo(C.Structure):
         ("nnz", C.c_uint64), ("block_count", C.c_uint64),
         ("dims", C.c_uint32 * GTK_MAX_ORDER), ("partition_dims", C.c_uint32 * GTK_MAX_ORDER),
         ("block_dims", C.c_uint32 * GTK_MAX_ORDER), ("norm", C.c_double), ("device_bytes", C.c_uint64),
-        ("streamed", C.c_uint32), ("stream_chunk", C.c_uint64),
+        ("streamed", C.c_uint32), ("stream_chunk", C.c_uint64), ("host_direct", C.c_uint32),
     ]
 
 

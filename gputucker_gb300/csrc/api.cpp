@@ -578,6 +578,7 @@ int gtk_tensor_info_get(const gtk_tensor *t, gtk_tensor_info *info) {
   info->device_bytes = t->bytes;
   info->streamed = t->streamed ? 1 : 0;
   info->stream_chunk = t->chunk;
+  info->host_direct = t->create_direct ? 1 : 0;
   return 0;
 }
 

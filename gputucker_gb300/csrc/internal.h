@@ -211,6 +211,7 @@ struct DevTensor {
   // gtk_create_blocks, CUDA events on the stream: host-to-device upload of the
   // COO, then the partition and segmenting kernels (ms)
   double create_upload_ms = 0, create_kernels_ms = 0;
+  bool create_direct = false;  // the partition read the host COO in place (no upload)
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, tev0 = nullptr, tev1 = nullptr;
 
   std::vector<std::pair<void *, size_t>> allocs;  // device blocks of the handle and their sizes

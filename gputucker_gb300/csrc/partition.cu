@@ -337,6 +337,33 @@ template <class V> __device__ __forceinline__ V rec_get_val(const uint32_t (&w)[
   return (V)__longlong_as_double((long long)(((unsigned long long)w[7] << 32) | w[6]));
 }
 
+// The caller's COO read in place from host memory (a device that reaches
+// pageable host memory: Grace's address translation over NVLink-C2C): the
+// input-order record, the device copy of the value (val_in) and the block id of
+// every nonzero in one pass -- the upload, k_pack_records and k_block_id fused
+template <class V>
+__global__ void k_pack_records_host(Ptrs g, const V *__restrict__ val, int N, Dims dm, uint64_t n,
+                                    uint4 *__restrict__ rec, V *__restrict__ val_dev, uint32_t *__restrict__ bid,
+                                    uint32_t *__restrict__ iota) {
+  for (uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t w[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll
+    for (int k = 0; k < kRecMaxOrder; ++k)
+      if (k < N) w[k] = g.p[k][t];
+    uint64_t b = 0, mult = 1;
+    for (int k = N - 1; k >= 0; --k) {
+      b += (uint64_t)(w[k] / dm.bd[k]) * mult;
+      mult *= dm.P[k];
+    }
+    const V v = val[t];
+    rec_put_val<V>(w, v);
+    rec_store(rec, t, w);
+    val_dev[t] = v;
+    bid[t] = (uint32_t)b;
+    iota[t] = (uint32_t)t;
+  }
+}
+
 // input-order records from the uploaded coordinate arrays and values
 template <class V>
 __global__ void k_pack_records(Ptrs g, const V *__restrict__ val, int N, uint64_t n, uint4 *__restrict__ rec) {
@@ -526,31 +553,21 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
     }
   } ev_guard{ev};
   for (auto &e : ev) TRY(ck(cudaEventCreate(&e), "cudaEventCreate"));
-  TRY(ck(cudaEventRecord(ev[0], s), "cudaEventRecord"));
-  // upload COO
-  Ptrs gin;
-  for (int k = 0; k < N; ++k) {
-    void *p;
-    TRY(talloc(&p, n * 4));
-    if (n) TRY(ck(cudaMemcpyAsync(p, coo.idx[k].data(), n * 4, cudaMemcpyHostToDevice, s), "upload coords"));
-    gin.p[k] = (const uint32_t *)p;
+  // Where the device reads pageable host memory coherently (Grace: address
+  // translation over NVLink-C2C), the first kernel reads the caller's arrays in
+  // place (k_pack_records_host); elsewhere, or with GTK_HOST_DIRECT=0, they are
+  // uploaded first.  Either way the host arrays are read once.
+  int pageable = 0;
+  if (cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, t.dev) != cudaSuccess) {
+    cudaGetLastError();
+    pageable = 0;
   }
+  const char *hd = getenv("GTK_HOST_DIRECT");
+  const bool direct = pageable == 1 && !(hd && *hd == '0') && N <= kRecMaxOrder && n;
+  t.create_direct = direct;
   // the values stay on the device in input order: the reference's serial norm sums them in that order
   TRY(dalloc(t, &t.val_in, n * sizeof(V)));
   V *dval = reinterpret_cast<V *>(t.val_in);
-  if (n) TRY(ck(cudaMemcpyAsync(dval, coo.values(), n * sizeof(V), cudaMemcpyHostToDevice, s), "upload values"));
-
-  TRY(ck(cudaEventRecord(ev[1], s), "cudaEventRecord"));
-  SortScratch sc;
-  const uint64_t ntiles = (n + kRsTile - 1) / kRsTile;
-  TRY(talloc((void **)&sc.k2, n * 4));
-  TRY(talloc((void **)&sc.v2, n * 4));
-  TRY(talloc((void **)&sc.hist, 256 * ntiles * 4 + 16));
-  uint64_t max_scan = std::max<uint64_t>(256 * ntiles, 1);
-  for (int k = 0; k < N; ++k) max_scan = std::max<uint64_t>(max_scan, t.nblk * (uint64_t)(t.bd[k] + 1));
-  max_scan = std::max<uint64_t>(max_scan, t.nblk + 1);
-  TRY(talloc((void **)&sc.sums, ((max_scan + kScanChunk - 1) / kScanChunk + 1) * 8));
-
   // 32-byte records (N <= 5): input order, then block order; without room for
   // them the gathers read the coordinate arrays one by one
   uint4 *rin = nullptr, *rblk = nullptr;
@@ -563,15 +580,45 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
       if (rblk) tmp.push_back({rblk, rb});
     }
     if (!rblk) rin = nullptr;
-    if (rin) {
-      k_pack_records<V><<<G, T, 0, s>>>(gin, dval, N, n, rin);
-      TRY(ck(cudaGetLastError(), "k_pack_records"));
-    }
   }
   uint32_t *sbid, *perm;
   TRY(talloc((void **)&sbid, n * 4));
   TRY(talloc((void **)&perm, n * 4));
-  if (n) {
+  TRY(ck(cudaEventRecord(ev[0], s), "cudaEventRecord"));
+  Ptrs gin;
+  const bool fused = direct && rin;
+  if (fused) {
+    Ptrs hst;
+    for (int k = 0; k < N; ++k) hst.p[k] = coo.idx[k].data();
+    k_pack_records_host<V><<<G, T, 0, s>>>(hst, reinterpret_cast<const V *>(coo.values()), N, dm, n, rin, dval, sbid,
+                                           perm);
+    TRY(ck(cudaGetLastError(), "k_pack_records_host"));
+  } else {
+    // upload COO
+    for (int k = 0; k < N; ++k) {
+      void *p;
+      TRY(talloc(&p, n * 4));
+      if (n) TRY(ck(cudaMemcpyAsync(p, coo.idx[k].data(), n * 4, cudaMemcpyHostToDevice, s), "upload coords"));
+      gin.p[k] = (const uint32_t *)p;
+    }
+    if (n) TRY(ck(cudaMemcpyAsync(dval, coo.values(), n * sizeof(V), cudaMemcpyHostToDevice, s), "upload values"));
+  }
+  TRY(ck(cudaEventRecord(ev[1], s), "cudaEventRecord"));
+  SortScratch sc;
+  const uint64_t ntiles = (n + kRsTile - 1) / kRsTile;
+  TRY(talloc((void **)&sc.k2, n * 4));
+  TRY(talloc((void **)&sc.v2, n * 4));
+  TRY(talloc((void **)&sc.hist, 256 * ntiles * 4 + 16));
+  uint64_t max_scan = std::max<uint64_t>(256 * ntiles, 1);
+  for (int k = 0; k < N; ++k) max_scan = std::max<uint64_t>(max_scan, t.nblk * (uint64_t)(t.bd[k] + 1));
+  max_scan = std::max<uint64_t>(max_scan, t.nblk + 1);
+  TRY(talloc((void **)&sc.sums, ((max_scan + kScanChunk - 1) / kScanChunk + 1) * 8));
+
+  if (rin && !fused) {
+    k_pack_records<V><<<G, T, 0, s>>>(gin, dval, N, n, rin);
+    TRY(ck(cudaGetLastError(), "k_pack_records"));
+  }
+  if (n && !fused) {
     k_block_id<<<G, T, 0, s>>>(gin, N, dm, n, sbid, perm);
     TRY(ck(cudaGetLastError(), "k_block_id"));
   }

@@ -466,8 +466,10 @@ __global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, con
 }
 
 // The precision form's row solve: FP32 Cholesky per thread (GB300 runs FP32 at
-// ~64x its FP64 rate), a condition estimate kappa ~ (max u_kk / min u_kk)^2 from
-// the factor, and one step of iterative refinement whose residual
+// ~64x its FP64 rate), a 1-norm condition estimate kappa_1 = ||B||_1 est(||B^-1||_1)
+// from the factor (Hager's method as refined by Higham, the estimator of
+// LAPACK's xPOCON: at most three rounds of two solves with U^T U), and one step
+// of iterative refinement whose residual
 // r = C - (lambda I + G) a is formed from the FP64 Gram with each entry split
 // into two floats, error-free products (fmaf) and Neumaier sums.  Rows with
 // kappa above cond_max, or a non-positive pivot, go to the FP64 solver.
@@ -475,6 +477,50 @@ __device__ __forceinline__ void neu_add(float &s, float &c, float x) {
   const float t = s + x;
   c += (fabsf(s) >= fabsf(x)) ? ((s - t) + x) : ((x - t) + s);
   s = t;
+}
+
+// y <- (U^T U)^-1 y in place (U packed at U[e * T], vectors strided by T)
+__device__ __forceinline__ void chol_solve32(const float *U, float *y, int J, int T) {
+  for (int k = 0; k < J; ++k) {  // U^T z = y
+    float v = y[k * T];
+    for (int p = 0; p < k; ++p) v -= U[upk(p, k, J) * T] * y[p * T];
+    y[k * T] = v / U[upk(k, k, J) * T];
+  }
+  for (int k = J - 1; k >= 0; --k) {  // U w = z
+    float v = y[k * T];
+    for (int j = k + 1; j < J; ++j) v -= U[upk(k, j, J) * T] * y[j * T];
+    y[k * T] = v / U[upk(k, k, J) * T];
+  }
+}
+
+// Hager/Higham estimate of ||B^-1||_1 for SPD B = U^T U: a lower bound, in
+// practice within a small factor (x, y: J-vector scratch strided by T)
+__device__ float inv_norm1_est(const float *U, float *x, float *y, int J, int T) {
+  for (int i = 0; i < J; ++i) x[i * T] = 1.f / (float)J;
+  float est = 0.f;
+  for (int it = 0; it < 3; ++it) {
+    for (int i = 0; i < J; ++i) y[i * T] = x[i * T];
+    chol_solve32(U, y, J, T);
+    float n1 = 0.f;
+    for (int i = 0; i < J; ++i) n1 += fabsf(y[i * T]);
+    if (it > 0 && n1 <= est) break;
+    est = n1;
+    float zx = 0.f;  // z = B^-1 sign(y) (B symmetric), z . x, argmax |z|
+    for (int i = 0; i < J; ++i) y[i * T] = y[i * T] >= 0.f ? 1.f : -1.f;
+    chol_solve32(U, y, J, T);
+    int jmax = 0;
+    float zmax = -1.f;
+    for (int i = 0; i < J; ++i) {
+      zx += y[i * T] * x[i * T];
+      if (fabsf(y[i * T]) > zmax) {
+        zmax = fabsf(y[i * T]);
+        jmax = i;
+      }
+    }
+    if (it > 0 && zmax <= zx) break;
+    for (int i = 0; i < J; ++i) x[i * T] = i == jmax ? 1.f : 0.f;
+  }
+  return est;
 }
 
 template <class V>
@@ -485,13 +531,20 @@ __global__ void k_solve_rows32(const double *__restrict__ gram, uint64_t rows, i
   const int T = blockDim.x, tid = threadIdx.x;
   float *U = sf + tid;                    // packed factor, element e at U[e * T]
   float *r = sf + (size_t)E * T + tid;    // residual / correction, element i at r[i * T]
+  float *w = sf + (size_t)(E + J) * T + tid;  // estimator scratch: two J-vectors
   const float lam = (float)lambda;
   for (uint64_t row = (uint64_t)blockIdx.x * T + tid; row < rows; row += (uint64_t)gridDim.x * T) {
     const double *g = gram + row * (uint64_t)E;
     for (int e = 0; e < E; ++e) U[e * T] = (float)g[e];
     for (int i = 0; i < J; ++i) U[upk(i, i, J) * T] = (float)(g[upk(i, i, J)] + lambda);
+    // ||B||_1 (B symmetric: the largest absolute row sum), from the FP64 Gram
+    float bnorm1 = 0.f;
+    for (int i = 0; i < J; ++i) {
+      double rs = 0;
+      for (int j = 0; j < J; ++j) rs += fabs(g[i <= j ? upk(i, j, J) : upk(j, i, J)]);
+      bnorm1 = fmaxf(bnorm1, (float)(rs + lambda));
+    }
     bool ok = true;
-    float umax = 0.f, umin = 3.4e38f;
     for (int k = 0; k < J; ++k) {
       const float d = U[upk(k, k, J) * T];
       if (!(d > 0.f) || !isfinite(d)) {
@@ -499,8 +552,6 @@ __global__ void k_solve_rows32(const double *__restrict__ gram, uint64_t rows, i
         break;
       }
       const float u = sqrtf(d), ru = 1.f / u;
-      umax = fmaxf(umax, u);
-      umin = fminf(umin, u);
       U[upk(k, k, J) * T] = u;
       for (int j = k + 1; j <= J; ++j) U[upk(k, j, J) * T] *= ru;
       for (int i = k + 1; i < J; ++i) {
@@ -508,7 +559,8 @@ __global__ void k_solve_rows32(const double *__restrict__ gram, uint64_t rows, i
         for (int j = i; j <= J; ++j) U[upk(i, j, J) * T] -= uki * U[upk(k, j, J) * T];
       }
     }
-    if (!ok || (umax / umin) * (umax / umin) > cond_max) {
+    const float kappa = ok ? bnorm1 * inv_norm1_est(U, w, w + (size_t)J * T, J, T) : 0.f;
+    if (!ok || !(kappa <= cond_max)) {
       to_fp64[atomicAdd(n_to_fp64, 1u)] = (uint32_t)row;
       atomicAdd(n_to_fp64 + 1, 1u);  // running count of the handle (gtk_solve_counters)
       continue;
@@ -935,8 +987,8 @@ template <class V, int KIND, int NPT> bool find_spec(Launch &L, const DevTensor 
 
 constexpr size_t kSmemLimit = 227 * 1024;
 constexpr int kThreadSolveMaxJ = 24;  // larger ranks solve one row per warp
-// precision form: rows whose Cholesky factor shows (max u_kk / min u_kk)^2 above
-// this are solved in FP64 (one FP32 refinement step leaves ~(kappa * 2^-24)^2)
+// precision form: rows whose 1-norm condition estimate exceeds this are solved
+// in FP64 (one FP32 refinement step leaves ~(kappa * 2^-24)^2)
 constexpr float kCondMaxFp32 = 1e5f;
 
 // kernel of a KIND: the update honours the handle's variant (set by the autotuner);
@@ -1209,7 +1261,7 @@ template <class V> static int update_impl(DevTensor &t, int mode) {
     if (grid < 1) grid = 1;
     if (t.precision != GTK_PREC_PLAIN) {
       // FP32 Cholesky + refinement; rows above the condition threshold in FP64
-      const size_t smem32 = (size_t)T * (E + J) * 4;
+      const size_t smem32 = (size_t)T * (E + 3 * J) * 4;
       if (int rc = prepare_fn((const void *)k_solve_rows32<V>, smem32)) return rc;
       GTK_CUDA(cudaMemsetAsync(t.nfallback + 1, 0, 4, t.stream));
       k_solve_rows32<V><<<(unsigned)grid, T, smem32, t.stream>>>(t.gram, t.rows[mode], J, E, t.ldf,

@@ -152,6 +152,7 @@ class Info:
     device_bytes: int
     streamed: bool = False
     stream_chunk: int = 0
+    host_direct: bool = False
 
 
 class BlockedTensor:
@@ -176,7 +177,7 @@ class BlockedTensor:
         n = ti.order
         return Info(ti.order, ti.rank, ti.dtype, ti.device, ti.nnz, ti.block_count, list(ti.dims[:n]),
                     list(ti.partition_dims[:n]), list(ti.block_dims[:n]), ti.norm, ti.device_bytes,
-                    bool(ti.streamed), ti.stream_chunk)
+                    bool(ti.streamed), ti.stream_chunk, bool(ti.host_direct))
 
     # ---- partition readback (bit-exact with the reference's blocks)
     def block(self, b: int):

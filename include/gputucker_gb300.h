@@ -77,6 +77,7 @@ typedef struct gtk_tensor_info {
   uint64_t device_bytes;              /* HBM held by the handle */
   uint32_t streamed;                  /* 1: the streamed layout (views in host memory, see gtk_create_blocks) */
   uint64_t stream_chunk;              /* nonzeros per device staging buffer of the streamed layout */
+  uint32_t host_direct;               /* 1: gtk_create_blocks read the host COO in place (no upload copy) */
 } gtk_tensor_info;
 
 /* ---- errors / version ------------------------------------------------- */
@@ -106,7 +107,10 @@ void gtk_coo_free(gtk_coo *coo);
 
 /* ---- blocking: replaces CreateTensorBlocks (tensor_manager.tpp:201-302) +
  *      Tensor::AssignIndicesOfEachBlock (tensor.tpp:139-147, block.tpp:115-186).
- * Uploads the COO to HBM and, on the GPU, assigns block ids (last mode fastest),
+ * Reads the COO into HBM -- in place from host memory where the device reaches
+ * pageable host memory (Grace: NVLink-C2C address translation; GTK_HOST_DIRECT=0
+ * uploads a copy instead), else by an upload -- and, on the GPU, assigns block
+ * ids (last mode fastest),
  * stable-sorts nonzeros into blocks in input order, stores block-local coords,
  * builds the per-mode count_nnz / where_nnz of every block (bit-exact with the
  * reference) and the per-mode row-sorted views the sweep runs on.
@@ -374,8 +378,9 @@ int gtk_write_text(const gtk_coo *coo, const char *path);
  * No reference counterpart (the reference inverts every B by LU in FP64,
  * update.cuh:163-194).  Rows solved by a fallback since the handle was created
  * or the counters were last reset: fp64_rows -- rows of the precision forms
- * whose FP32 Cholesky showed a condition estimate (max u_kk / min u_kk)^2 above
- * 1e5, or a non-positive pivot, and were re-solved by FP64 Cholesky; lu_rows --
+ * whose 1-norm condition estimate ||B||_1 est(||B^-1||_1) (Hager/Higham, from
+ * the FP32 Cholesky factor) exceeded 1e5, or whose FP32 Cholesky met a
+ * non-positive pivot, and were re-solved by FP64 Cholesky; lu_rows --
  * rows whose FP64 Cholesky met a non-positive pivot and were solved by LU with
  * partial pivoting.  reset != 0 zeroes both after reading. */
 int gtk_solve_counters(gtk_tensor *t, uint64_t *fp64_rows, uint64_t *lu_rows, int reset);

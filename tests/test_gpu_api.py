@@ -94,15 +94,20 @@ def test_state_error_before_init():
 
 
 def test_memory_cap_reports_oom(monkeypatch):
-    """An allocation cap (GTK_DEVICE_MEMORY_CAP) stands in for an exhausted HBM."""
+    """An allocation cap (GTK_DEVICE_MEMORY_CAP) stands in for an exhausted HBM: a cap
+    below the resident layout gives the streamed layout, a cap below even the
+    factors and Gram/RHS that the streamed layout keeps resident is GTK_ERR_OOM."""
     coo = gtk.generate(3, [1000] * 3, 100_000, "uniform", 0, "uniform", "f32", seed=1)
-    monkeypatch.setenv("GTK_DEVICE_MEMORY_CAP", str(1 << 20))
+    monkeypatch.setenv("GTK_DEVICE_MEMORY_CAP", str(1 << 16))
     with pytest.raises(gtk.GTKError) as e:
         gtk.create_tensor_blocks(coo, [1, 1, 1], 8)
     assert e.value.code == nat.GTK_ERR_OOM
+    monkeypatch.setenv("GTK_DEVICE_MEMORY_CAP", str(1 << 20))
+    with gtk.create_tensor_blocks(coo, [1, 1, 1], 8) as t:
+        assert t.info.streamed and t.info.device_bytes <= (1 << 20)
     monkeypatch.delenv("GTK_DEVICE_MEMORY_CAP")
     with gtk.create_tensor_blocks(coo, [1, 1, 1], 8) as t:
-        assert t.info.device_bytes > (1 << 20)
+        assert not t.info.streamed and t.info.device_bytes > (1 << 20)
 
 
 def test_direct_fit_after_set_factor_matches_stored_delta_fit():
@@ -201,3 +206,32 @@ def test_cached_device_blocks_are_reused_cleanly():
     gtk.release_cached_memory()
     free_after, _ = gtk.device_memory()
     assert abs(free_after - free_cached) <= total // 100, (free_cached, free_after)
+
+
+def test_host_direct_read_matches_upload(monkeypatch):
+    """The partition reading the host COO in place (where the device reaches pageable
+    host memory) and the one reading an uploaded copy give identical handles."""
+    from oracle_util import random_coo
+    rng = np.random.default_rng(9)
+    dims, P = [60, 50, 40, 30], [2, 2, 1, 3]
+    idx = random_coo(rng, dims, 20_000, distinct=True, zipf=1.1)
+    vals = rng.random(len(idx[0])).astype(np.float32)
+    coo = gtk.coo_from_arrays(idx, vals, dims=dims)
+    monkeypatch.setenv("GTK_HOST_DIRECT", "0")
+    with gtk.create_tensor_blocks(coo, P, 8) as up:
+        assert not up.info.host_direct
+        monkeypatch.delenv("GTK_HOST_DIRECT")
+        with gtk.create_tensor_blocks(coo, P, 8) as dr:
+            print("host_direct", dr.info.host_direct)
+            assert dr.info.norm == up.info.norm
+            for b in range(dr.info.block_count):
+                c1, i1, v1 = dr.block(b)
+                c2, i2, v2 = up.block(b)
+                assert c1 == c2 and np.array_equal(v1, v2)
+                assert all(np.array_equal(x, y) for x, y in zip(i1, i2))
+                for n in range(4):
+                    s1, s2 = dr.segments(b, n), up.segments(b, n)
+                    assert np.array_equal(s1[0], s2[0]) and np.array_equal(s1[1], s2[1])
+            for t in (dr, up):
+                t.init_random(1, 0)
+            assert abs(dr.sweep() - up.sweep()) <= 1e-6  # FP64 atomic adds in either order
