@@ -40,6 +40,20 @@ struct ModeArgs {
   const void *core;                  // the core, linear order (last mode fastest): ref_order
 };
 
+// the entry i of a multi-tensor launch whose CTA range [first[i], first[i + 1])
+// holds CTA b (first[0] = 0, first[count] = the grid)
+__device__ __forceinline__ int slot_of(const uint32_t *__restrict__ first, int count, uint32_t b) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(first + mid) <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 // ---------------------------------------------------------------- vector loads
 template <class V> struct Vec;
 template <> struct Vec<float> {

@@ -117,8 +117,8 @@ template <int N, int J, int LDG> struct CoreStream {
 // ---------------------------------------------------------------- specialised kernel
 // Compile-time order N and rank J; NPT nonzeros per thread share every core read.
 // STREAM: the core is streamed through shared memory in chunks (CoreStream).
-template <class V, int N, int J, int NPT, int KIND, bool STREAM = false>
-__global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
+template <class V, int N, int J, int NPT, int KIND, bool STREAM>
+__device__ __forceinline__ void mode_spec_body(const ModeArgs &a, uint32_t cta, uint32_t nctas) {
   using VT = typename Vec<V>::T;
   constexpr int W = Vec<V>::W;
   constexpr int LDG = (J + W - 1) / W * W;  // equals the factor row stride ldf
@@ -147,9 +147,9 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
   if (KIND == kUpdate) gram.init(s.pi, s.pj, a.E, J + 1, tid & 31);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + TN - 1) / TN;
-  const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
-  const uint64_t tile_end = min(ntiles, (uint64_t)(blockIdx.x + 1) * per);
-  for (uint64_t tile = (uint64_t)blockIdx.x * per; tile < tile_end; ++tile) {
+  const uint64_t per = (ntiles + nctas - 1) / nctas;
+  const uint64_t tile_end = min(ntiles, (uint64_t)(cta + 1) * per);
+  for (uint64_t tile = (uint64_t)cta * per; tile < tile_end; ++tile) {
     __syncthreads();  // previous tile's reduction is done with the shared tile
     const uint64_t t0 = tile * TN;
     const int nv = (int)min((uint64_t)TN, a.nnz - t0);
@@ -275,8 +275,22 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
   if (KIND == kUpdate) gram.flush(a.gram, a.E, tid & 31);
   if (KIND == kFit) {
     const double tot = block_sum(err);
-    if (tid == 0) a.partial[blockIdx.x] = tot;
+    if (tid == 0) a.partial[cta] = tot;
   }
+}
+
+template <class V, int N, int J, int NPT, int KIND, bool STREAM = false>
+__global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
+  mode_spec_body<V, N, J, NPT, KIND, STREAM>(a, blockIdx.x, gridDim.x);
+}
+
+// Many tensors of one shape class in one launch (batches): CTA b works for
+// tensor i with cta_first[i] <= b < cta_first[i + 1], on that tensor's tiles
+template <class V, int N, int J, int NPT, int KIND, bool STREAM = false>
+__global__ void __launch_bounds__(kThreads)
+    k_mode_spec_multi(const ModeArgs *__restrict__ args, const uint32_t *__restrict__ cta_first, int count) {
+  const int i = slot_of(cta_first, count, blockIdx.x);
+  mode_spec_body<V, N, J, NPT, KIND, STREAM>(args[i], blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
 }
 
 // ---------------------------------------------------------------- generic kernel

@@ -102,7 +102,8 @@ __device__ __forceinline__ bool wait_bounded(uint64_t *bar, uint32_t parity) {
 }
 
 template <int N, int J, int KIND>
-__global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const unsigned char *__restrict__ bimg) {
+__device__ __forceinline__ void mode_tcs_body(const ModeArgs &a, const unsigned char *__restrict__ bimg, uint32_t cta,
+                                              uint32_t nctas) {
   using S = TsShape<N, J>;
   constexpr int D = S::D;
   constexpr int LDG = (J + 3) / 4 * 4;  // factor row stride (floats)
@@ -141,8 +142,8 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
   if (KIND == 0) gram.init(tid & 31);
 
   const uint64_t ntiles = (a.nnz + kTsThreads - 1) / kTsThreads;
-  const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
-  const uint64_t tile_begin = (uint64_t)blockIdx.x * per;
+  const uint64_t per = (ntiles + nctas - 1) / nctas;
+  const uint64_t tile_begin = (uint64_t)cta * per;
   const uint64_t tile_end = min(ntiles, tile_begin + per);
   const uint64_t total = tile_begin < tile_end ? (tile_end - tile_begin) * S::NCH : 0;
   // thread 0's record of what is in flight: the last chunk copied and the last MMA group
@@ -348,7 +349,7 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
     if (KIND == 0) gram.flush(a.gram, S::E, tid & 31);
     if (KIND == 1) {
       const double tot = block_sum(err);
-      if (tid == 0) a.partial[blockIdx.x] = tot;
+      if (tid == 0) a.partial[cta] = tot;
     }
   }
   tc_fence_before();
@@ -357,6 +358,21 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
     tc_fence_after();
     tmem_dealloc(tmem, 2 * S::NCOLS);
   }
+}
+
+template <int N, int J, int KIND>
+__global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const unsigned char *__restrict__ bimg) {
+  mode_tcs_body<N, J, KIND>(a, bimg, blockIdx.x, gridDim.x);
+}
+
+// many tensors of one shape class in one launch (batches), as k_mode_spec_multi;
+// bimgs[i]: tensor i's core image of the mode
+template <int N, int J, int KIND>
+__global__ void __launch_bounds__(kTsThreads, 1)
+    k_mode_tcs_multi(const ModeArgs *__restrict__ args, const unsigned char *const *__restrict__ bimgs,
+                     const uint32_t *__restrict__ cta_first, int count) {
+  const int i = slot_of(cta_first, count, blockIdx.x);
+  mode_tcs_body<N, J, KIND>(args[i], bimgs[i], blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
 }
 
 struct TsLaunch {

@@ -80,7 +80,7 @@ template <int J, int D, int PREC> struct TcShape {
 
 
 template <int J, int D, int PREC, int KIND>
-__global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
+__device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, uint32_t nctas) {
   using S = TcShape<J, D, PREC>;
   constexpr int LDG = (J + 3) / 4 * 4;  // factor row stride (floats)
   extern __shared__ __align__(1024) unsigned char smem[];
@@ -132,8 +132,8 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   if (KIND == 0) gram.init(lane);
   // a contiguous range of tiles per CTA, so a warp's running Gram sums follow a row across tiles
   const uint64_t ntiles = (a.nnz + kTcThreads - 1) / kTcThreads;
-  const uint64_t per = (ntiles + gridDim.x - 1) / gridDim.x;
-  const uint64_t tile_end = min(ntiles, (uint64_t)(blockIdx.x + 1) * per);
+  const uint64_t per = (ntiles + nctas - 1) / nctas;
+  const uint64_t tile_end = min(ntiles, (uint64_t)(cta + 1) * per);
   // inputs of one tile for this thread: its nonzero's row, value and the factor
   // rows (p, q form the Kronecker operand; e1 (D = 3) finishes the contraction).
   // Loaded in two stages a tile apart -- the coordinates two tiles ahead, the
@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   };
   TileIn cur;
   TileCrd crd;  // coordinates of the tile after `cur`
-  const uint64_t tile_begin = (uint64_t)blockIdx.x * per;
+  const uint64_t tile_begin = (uint64_t)cta * per;
   if (tile_begin < tile_end) {
     load_crd(tile_begin, crd);
     load_rows(crd, cur);
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
   if (KIND == 0 && !timed_out) gram.flush(a.gram, S::E, lane);
   if (KIND == 1) {
     const double tot = block_sum(err);
-    if (tid == 0) a.partial[blockIdx.x] = tot;
+    if (tid == 0) a.partial[cta] = tot;
   }
   tc_fence_before();
   __syncthreads();
@@ -346,6 +346,19 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
     tc_fence_after();
     tmem_dealloc(tmem, S::NCOLS);
   }
+}
+
+template <int J, int D, int PREC, int KIND>
+__global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
+  mode_tc_body<J, D, PREC, KIND>(a, blockIdx.x, gridDim.x);
+}
+
+// many tensors of one shape class in one launch (batches), as k_mode_spec_multi
+template <int J, int D, int PREC, int KIND>
+__global__ void __launch_bounds__(kTcThreads)
+    k_mode_tc_multi(const ModeArgs *__restrict__ args, const uint32_t *__restrict__ cta_first, int count) {
+  const int i = slot_of(cta_first, count, blockIdx.x);
+  mode_tc_body<J, D, PREC, KIND>(args[i], blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
 }
 
 struct TcLaunch {
