@@ -52,6 +52,9 @@ struct gtk_batch {
   cudaGraphExec_t gexec = nullptr;
   uint64_t graph_kernels = 0;
   bool warmed = false;
+  gtk::FusedBatch *fused = nullptr;  // the few-launch form of the sweep, when every handle has one
+  uint64_t fused_kernels = 0;
+  std::vector<std::pair<int, int>> fused_for;  // (precision, variant) of each handle the plan was built for
 };
 
 using namespace gtk;
@@ -102,6 +105,12 @@ double *out_err(gtk_batch *b) { return static_cast<double *>(b->d_out); }
 int *out_status(gtk_batch *b) { return reinterpret_cast<int *>(out_err(b) + b->count); }
 
 int batch_enqueue(gtk_batch *b) {
+  if (b->fused) {
+    uint64_t k = 0;
+    if (int rc = fused_batch_enqueue(b->fused, b->stream, out_err(b), out_status(b), &k)) return rc;
+    b->fused_kernels = k;
+    return 0;
+  }
   GTK_CUDA(cudaEventRecord(b->fork, b->stream));
   for (int i = 0; i < b->count; ++i) {
     gtk_tensor *t = b->ts[i];
@@ -125,6 +134,13 @@ void drop_batch_graph(gtk_batch *b) {
   b->gexec = nullptr;
   b->graph = nullptr;
   b->graph_kernels = 0;
+  // the fused plan holds each handle's kernel choice: rebuilt (eagerly) at the next sweep
+  if (b->fused) {
+    cudaStreamSynchronize(b->stream);
+    fused_batch_free(b->fused);
+    b->fused = nullptr;
+    b->warmed = false;
+  }
 }
 
 int capture(gtk_batch *b) {
@@ -139,9 +155,9 @@ int capture(gtk_batch *b) {
   const int rc = batch_enqueue(b);
   cudaGraph_t g = nullptr;
   const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
-  uint64_t kernels = 1;  // the gather kernel
+  uint64_t kernels = b->fused ? b->fused_kernels : 1;  // fused: every kernel; else the gather kernel + the handles'
   for (int i = 0; i < b->count; ++i) {
-    kernels += b->ts[i]->launches - l0[i];
+    if (!b->fused) kernels += b->ts[i]->launches - l0[i];
     b->ts[i]->launches = l0[i];
     b->ts[i]->prof = prof[i];
   }
@@ -304,11 +320,26 @@ int gtk_batch_sweep(gtk_batch *b, double *fits) {
       for (int i = 0; i < b->count && b->gexec; ++i)
         if (b->captured[i] != std::make_pair(b->ts[i]->precision, b->ts[i]->variant)) drop_batch_graph(b);
     }
+    if (b->fused) {
+      for (int i = 0; i < b->count && b->fused; ++i)
+        if (b->fused_for[i] != std::make_pair(b->ts[i]->precision, b->ts[i]->variant)) drop_batch_graph(b);
+    }
     if (!b->warmed) {
       for (gtk_tensor *t : b->ts)
         if (sweep_needs_dstore(*t))
           if (int rc = ensure_dstore(*t)) return rc;
+      // the few-launch form where every handle has one (GTK_BATCH_FUSED=0: per-handle launches)
+      const char *fz = getenv("GTK_BATCH_FUSED");
+      if (!b->fused && !(fz && *fz == '0')) {
+        std::vector<DevTensor *> ts(b->ts.begin(), b->ts.end());
+        const int rc = fused_batch_build(ts, &b->fused);
+        if (rc && rc != GTK_ERR_UNSUPPORTED) return rc;
+        if (rc) set_error("");
+        b->fused_for.clear();
+        for (gtk_tensor *t : b->ts) b->fused_for.emplace_back(t->precision, t->variant);
+      }
       if (int rc = batch_enqueue(b)) return rc;
+      if (b->fused) b->graph_kernels = b->fused_kernels;  // the same launches the graph will hold
       b->warmed = true;
     } else {
       if (!b->gexec)
@@ -346,6 +377,7 @@ void gtk_batch_destroy(gtk_batch *b) {
   cudaSetDevice(b->dev);
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_batch_graph(b);
+  if (b->fused) fused_batch_free(b->fused);
   for (cudaEvent_t e : b->joins)
     if (e) cudaEventDestroy(e);
   if (b->fork) cudaEventDestroy(b->fork);

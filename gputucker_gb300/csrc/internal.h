@@ -275,6 +275,32 @@ struct DevBuf {
   template <class T> T *as() const { return static_cast<T *>(p); }
 };
 
+// ---- batches: kernels shared by many handles per launch (gtk_batch_sweep)
+constexpr size_t kModeArgsBytes = 320;
+// One handle's mode update in the form its kernel class's multi-tensor kernel takes
+struct MultiDesc {
+  const void *fn = nullptr;              // k_mode_*_multi<...> of the class
+  int threads = 0;
+  size_t smem = 0;
+  uint32_t ctas = 0;                     // this handle's share of the grid
+  bool with_image = false;               // streamed-core tensor-core class: a core-image table too
+  bool tmem = false;                     // the class allocates tensor memory (launched one class at a time)
+  const unsigned char *image = nullptr;
+  alignas(16) unsigned char args[kModeArgsBytes];  // the kernel's argument block for this handle
+};
+int tc_multi_desc(DevTensor &t, int mode, MultiDesc *d);  // tc_sweep.cu (defers to tc_stream.cu's classes)
+int ts_multi_desc(DevTensor &t, int mode, MultiDesc *d);  // tc_stream.cu
+// A sweep of many handles in few launches (sweep.cu): per mode index one kernel
+// zeroing every handle's Gram/RHS, one multi-tensor update launch per kernel
+// class (classes on side streams), one batched row solve and its FP64 and LU
+// list passes; then one fit launch and one reduction that also gathers the
+// status words.  fused_batch_build returns GTK_ERR_UNSUPPORTED when some handle
+// has no multi-tensor form (the caller then launches per handle).
+struct FusedBatch;
+int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out);
+int fused_batch_enqueue(FusedBatch *fb, cudaStream_t s, double *err_out, int *status_out, uint64_t *kernels);
+void fused_batch_free(FusedBatch *fb);
+
 // partition.cu
 int build_partition(DevTensor &t, const gtk_coo &coo);
 // hostpart.cpp: the blocked arrays and mode views of the streamed layout, in t.hp

@@ -433,6 +433,47 @@ __device__ __forceinline__ int upk(int i, int j, int J) {  // packed index of (i
   return i * (J + 1) - (i * (i - 1)) / 2 + (j - i);
 }
 
+// FP64 Cholesky of lambda I + Gram of one row, in the thread-interleaved shared
+// scratch A (element e at A[e * T]); the solution into the factor row, or the
+// row onto the pivoted-LU list when a pivot is not positive
+template <class V>
+__device__ __forceinline__ void solve_row64(const double *__restrict__ gram, uint64_t row, int J, int E, int ldf,
+                                            V *__restrict__ fac, double lambda, double *A, int T,
+                                            uint32_t *__restrict__ fallback, unsigned int *__restrict__ nfallback) {
+  const double *g = gram + row * (uint64_t)E;
+  for (int e = 0; e < E; ++e) A[e * T] = g[e];
+  for (int i = 0; i < J; ++i) A[upk(i, i, J) * T] += lambda;
+  bool ok = true;
+  for (int k = 0; k < J && ok; ++k) {
+    const double d = A[upk(k, k, J) * T];
+    if (!(d > 0.0) || !isfinite(d)) {
+      ok = false;
+      break;
+    }
+    const double u = sqrt(d), r = 1.0 / u;
+    A[upk(k, k, J) * T] = u;
+    for (int j = k + 1; j <= J; ++j) A[upk(k, j, J) * T] *= r;  // row k of U, and C_k / u_kk
+    for (int i = k + 1; i < J; ++i) {
+      const double uki = A[upk(k, i, J) * T];
+      for (int j = i; j <= J; ++j) A[upk(i, j, J) * T] -= uki * A[upk(k, j, J) * T];
+    }
+  }
+  // the elimination above also carried C through U^T y = C: column J now holds y
+  V *frow = fac + row * (uint64_t)ldf;
+  if (ok) {
+    for (int k = J - 1; k >= 0; --k) {
+      double v = A[upk(k, J, J) * T];
+      for (int j = k + 1; j < J; ++j) v -= A[upk(k, j, J) * T] * A[upk(j, J, J) * T];
+      v /= A[upk(k, k, J) * T];
+      A[upk(k, J, J) * T] = v;
+    }
+    for (int j = 0; j < ldf; ++j) frow[j] = j < J ? (V)A[upk(j, J, J) * T] : V(0);
+  } else {
+    fallback[atomicAdd(nfallback, 1u)] = (uint32_t)row;
+    atomicAdd(nfallback + 3, 1u);  // running count of the handle (gtk_solve_counters)
+  }
+}
+
 // list_in == nullptr: rows 0..rows-1; else the *nlist_in rows listed
 template <class V>
 __global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, const uint32_t *__restrict__ list_in,
@@ -440,43 +481,9 @@ __global__ void k_solve_rows(const double *__restrict__ gram, uint64_t rows, con
                              double lambda, uint32_t *__restrict__ fallback, unsigned int *__restrict__ nfallback) {
   extern __shared__ double sm[];
   const int T = blockDim.x, tid = threadIdx.x;
-  double *A = sm + tid;  // element e at A[e * T]
   const uint64_t n = list_in ? (uint64_t)*nlist_in : rows;
-  for (uint64_t k0 = (uint64_t)blockIdx.x * T + tid; k0 < n; k0 += (uint64_t)gridDim.x * T) {
-    const uint64_t row = list_in ? list_in[k0] : k0;
-    const double *g = gram + row * (uint64_t)E;
-    for (int e = 0; e < E; ++e) A[e * T] = g[e];
-    for (int i = 0; i < J; ++i) A[upk(i, i, J) * T] += lambda;
-    bool ok = true;
-    for (int k = 0; k < J && ok; ++k) {
-      const double d = A[upk(k, k, J) * T];
-      if (!(d > 0.0) || !isfinite(d)) {
-        ok = false;
-        break;
-      }
-      const double u = sqrt(d), r = 1.0 / u;
-      A[upk(k, k, J) * T] = u;
-      for (int j = k + 1; j <= J; ++j) A[upk(k, j, J) * T] *= r;  // row k of U, and C_k / u_kk
-      for (int i = k + 1; i < J; ++i) {
-        const double uki = A[upk(k, i, J) * T];
-        for (int j = i; j <= J; ++j) A[upk(i, j, J) * T] -= uki * A[upk(k, j, J) * T];
-      }
-    }
-    // the elimination above also carried C through U^T y = C: column J now holds y
-    V *frow = fac + row * (uint64_t)ldf;
-    if (ok) {
-      for (int k = J - 1; k >= 0; --k) {
-        double v = A[upk(k, J, J) * T];
-        for (int j = k + 1; j < J; ++j) v -= A[upk(k, j, J) * T] * A[upk(j, J, J) * T];
-        v /= A[upk(k, k, J) * T];
-        A[upk(k, J, J) * T] = v;
-      }
-      for (int j = 0; j < ldf; ++j) frow[j] = j < J ? (V)A[upk(j, J, J) * T] : V(0);
-    } else {
-      fallback[atomicAdd(nfallback, 1u)] = (uint32_t)row;
-      atomicAdd(nfallback + 3, 1u);  // running count of the handle (gtk_solve_counters)
-    }
-  }
+  for (uint64_t k0 = (uint64_t)blockIdx.x * T + tid; k0 < n; k0 += (uint64_t)gridDim.x * T)
+    solve_row64<V>(gram, list_in ? list_in[k0] : k0, J, E, ldf, fac, lambda, sm + tid, T, fallback, nfallback);
 }
 
 // The precision form's row solve: FP32 Cholesky per thread (GB300 runs FP32 at
@@ -537,86 +544,95 @@ __device__ float inv_norm1_est(const float *U, float *x, float *y, int J, int T)
   return est;
 }
 
+// FP32 Cholesky + condition estimate + one refinement step of one row (scratch
+// sf: (E + 3J) floats, thread-interleaved); rows above cond_max, or with a
+// non-positive pivot, onto the FP64 list
+template <class V>
+__device__ __forceinline__ void solve_row32(const double *__restrict__ gram, uint64_t row, int J, int E, int ldf,
+                                            V *__restrict__ fac, double lambda, float cond_max, float *sf, int T,
+                                            uint32_t *__restrict__ to_fp64, unsigned int *__restrict__ n_to_fp64) {
+  float *U = sf;                          // packed factor, element e at U[e * T]
+  float *r = sf + (size_t)E * T;          // residual / correction, element i at r[i * T]
+  float *w = sf + (size_t)(E + J) * T;    // estimator scratch: two J-vectors
+  const float lam = (float)lambda;
+  const double *g = gram + row * (uint64_t)E;
+  for (int e = 0; e < E; ++e) U[e * T] = (float)g[e];
+  for (int i = 0; i < J; ++i) U[upk(i, i, J) * T] = (float)(g[upk(i, i, J)] + lambda);
+  // ||B||_1 (B symmetric: the largest absolute row sum), from the FP64 Gram
+  float bnorm1 = 0.f;
+  for (int i = 0; i < J; ++i) {
+    double rs = 0;
+    for (int j = 0; j < J; ++j) rs += fabs(g[i <= j ? upk(i, j, J) : upk(j, i, J)]);
+    bnorm1 = fmaxf(bnorm1, (float)(rs + lambda));
+  }
+  bool ok = true;
+  for (int k = 0; k < J; ++k) {
+    const float d = U[upk(k, k, J) * T];
+    if (!(d > 0.f) || !isfinite(d)) {
+      ok = false;
+      break;
+    }
+    const float u = sqrtf(d), ru = 1.f / u;
+    U[upk(k, k, J) * T] = u;
+    for (int j = k + 1; j <= J; ++j) U[upk(k, j, J) * T] *= ru;
+    for (int i = k + 1; i < J; ++i) {
+      const float uki = U[upk(k, i, J) * T];
+      for (int j = i; j <= J; ++j) U[upk(i, j, J) * T] -= uki * U[upk(k, j, J) * T];
+    }
+  }
+  const float kappa = ok ? bnorm1 * inv_norm1_est(U, w, w + (size_t)J * T, J, T) : 0.f;
+  if (!ok || !(kappa <= cond_max)) {
+    to_fp64[atomicAdd(n_to_fp64, 1u)] = (uint32_t)row;
+    atomicAdd(n_to_fp64 + 1, 1u);  // running count of the handle (gtk_solve_counters)
+    return;
+  }
+  for (int k = J - 1; k >= 0; --k) {  // U a = y, a kept in column J
+    float v = U[upk(k, J, J) * T];
+    for (int j = k + 1; j < J; ++j) v -= U[upk(k, j, J) * T] * U[upk(j, J, J) * T];
+    U[upk(k, J, J) * T] = v / U[upk(k, k, J) * T];
+  }
+  // r = C - lambda a - G a, compensated
+  for (int i = 0; i < J; ++i) {
+    float s = 0.f, c = 0.f;
+    const double ci = g[upk(i, J, J)];
+    const float ch = (float)ci;
+    neu_add(s, c, ch);
+    neu_add(s, c, (float)(ci - (double)ch));
+    const float ai = U[upk(i, J, J) * T];
+    neu_add(s, c, -lam * ai);
+    for (int j = 0; j < J; ++j) {
+      const double gij = g[i <= j ? upk(i, j, J) : upk(j, i, J)];
+      const float gh = (float)gij, gl = (float)(gij - (double)gh);
+      const float aj = U[upk(j, J, J) * T];
+      const float ph = gh * aj;
+      const float pl = fmaf(gh, aj, -ph);
+      neu_add(s, c, -ph);
+      neu_add(s, c, -(pl + gl * aj));
+    }
+    r[i * T] = s + c;
+  }
+  for (int k = 0; k < J; ++k) {  // U^T z = r
+    float v = r[k * T];
+    for (int p = 0; p < k; ++p) v -= U[upk(p, k, J) * T] * r[p * T];
+    r[k * T] = v / U[upk(k, k, J) * T];
+  }
+  for (int k = J - 1; k >= 0; --k) {  // U d = z
+    float v = r[k * T];
+    for (int j = k + 1; j < J; ++j) v -= U[upk(k, j, J) * T] * r[j * T];
+    r[k * T] = v / U[upk(k, k, J) * T];
+  }
+  V *frow = fac + row * (uint64_t)ldf;
+  for (int j = 0; j < ldf; ++j) frow[j] = j < J ? (V)(U[upk(j, J, J) * T] + r[j * T]) : V(0);
+}
+
 template <class V>
 __global__ void k_solve_rows32(const double *__restrict__ gram, uint64_t rows, int J, int E, int ldf,
                                V *__restrict__ fac, double lambda, float cond_max, uint32_t *__restrict__ to_fp64,
                                unsigned int *__restrict__ n_to_fp64) {
   extern __shared__ float sf[];
   const int T = blockDim.x, tid = threadIdx.x;
-  float *U = sf + tid;                    // packed factor, element e at U[e * T]
-  float *r = sf + (size_t)E * T + tid;    // residual / correction, element i at r[i * T]
-  float *w = sf + (size_t)(E + J) * T + tid;  // estimator scratch: two J-vectors
-  const float lam = (float)lambda;
-  for (uint64_t row = (uint64_t)blockIdx.x * T + tid; row < rows; row += (uint64_t)gridDim.x * T) {
-    const double *g = gram + row * (uint64_t)E;
-    for (int e = 0; e < E; ++e) U[e * T] = (float)g[e];
-    for (int i = 0; i < J; ++i) U[upk(i, i, J) * T] = (float)(g[upk(i, i, J)] + lambda);
-    // ||B||_1 (B symmetric: the largest absolute row sum), from the FP64 Gram
-    float bnorm1 = 0.f;
-    for (int i = 0; i < J; ++i) {
-      double rs = 0;
-      for (int j = 0; j < J; ++j) rs += fabs(g[i <= j ? upk(i, j, J) : upk(j, i, J)]);
-      bnorm1 = fmaxf(bnorm1, (float)(rs + lambda));
-    }
-    bool ok = true;
-    for (int k = 0; k < J; ++k) {
-      const float d = U[upk(k, k, J) * T];
-      if (!(d > 0.f) || !isfinite(d)) {
-        ok = false;
-        break;
-      }
-      const float u = sqrtf(d), ru = 1.f / u;
-      U[upk(k, k, J) * T] = u;
-      for (int j = k + 1; j <= J; ++j) U[upk(k, j, J) * T] *= ru;
-      for (int i = k + 1; i < J; ++i) {
-        const float uki = U[upk(k, i, J) * T];
-        for (int j = i; j <= J; ++j) U[upk(i, j, J) * T] -= uki * U[upk(k, j, J) * T];
-      }
-    }
-    const float kappa = ok ? bnorm1 * inv_norm1_est(U, w, w + (size_t)J * T, J, T) : 0.f;
-    if (!ok || !(kappa <= cond_max)) {
-      to_fp64[atomicAdd(n_to_fp64, 1u)] = (uint32_t)row;
-      atomicAdd(n_to_fp64 + 1, 1u);  // running count of the handle (gtk_solve_counters)
-      continue;
-    }
-    for (int k = J - 1; k >= 0; --k) {  // U a = y, a kept in column J
-      float v = U[upk(k, J, J) * T];
-      for (int j = k + 1; j < J; ++j) v -= U[upk(k, j, J) * T] * U[upk(j, J, J) * T];
-      U[upk(k, J, J) * T] = v / U[upk(k, k, J) * T];
-    }
-    // r = C - lambda a - G a, compensated
-    for (int i = 0; i < J; ++i) {
-      float s = 0.f, c = 0.f;
-      const double ci = g[upk(i, J, J)];
-      const float ch = (float)ci;
-      neu_add(s, c, ch);
-      neu_add(s, c, (float)(ci - (double)ch));
-      const float ai = U[upk(i, J, J) * T];
-      neu_add(s, c, -lam * ai);
-      for (int j = 0; j < J; ++j) {
-        const double gij = g[i <= j ? upk(i, j, J) : upk(j, i, J)];
-        const float gh = (float)gij, gl = (float)(gij - (double)gh);
-        const float aj = U[upk(j, J, J) * T];
-        const float ph = gh * aj;
-        const float pl = fmaf(gh, aj, -ph);
-        neu_add(s, c, -ph);
-        neu_add(s, c, -(pl + gl * aj));
-      }
-      r[i * T] = s + c;
-    }
-    for (int k = 0; k < J; ++k) {  // U^T z = r
-      float v = r[k * T];
-      for (int p = 0; p < k; ++p) v -= U[upk(p, k, J) * T] * r[p * T];
-      r[k * T] = v / U[upk(k, k, J) * T];
-    }
-    for (int k = J - 1; k >= 0; --k) {  // U d = z
-      float v = r[k * T];
-      for (int j = k + 1; j < J; ++j) v -= U[upk(k, j, J) * T] * r[j * T];
-      r[k * T] = v / U[upk(k, k, J) * T];
-    }
-    V *frow = fac + row * (uint64_t)ldf;
-    for (int j = 0; j < ldf; ++j) frow[j] = j < J ? (V)(U[upk(j, J, J) * T] + r[j * T]) : V(0);
-  }
+  for (uint64_t row = (uint64_t)blockIdx.x * T + tid; row < rows; row += (uint64_t)gridDim.x * T)
+    solve_row32<V>(gram, row, J, E, ldf, fac, lambda, cond_max, sf + tid, T, to_fp64, n_to_fp64);
 }
 
 // decode entry e of the packed row into (i, j), 0 <= i <= j <= J
@@ -955,6 +971,7 @@ __global__ void k_sum_fit(const double *__restrict__ partial, int m, double *__r
 // ---------------------------------------------------------------- dispatch
 struct Launch {
   const void *fn = nullptr;
+  const void *fn_multi = nullptr;  // the multi-tensor form (FP32 updates), for batches
   size_t smem = 0;
   int tn = 0;  // nonzeros per tile
   bool spec = false;
@@ -969,6 +986,8 @@ void spec_entry(Launch &L, const DevTensor &t) {
   constexpr int LEV = D > 2 ? D - 2 : 0;
   const size_t gp = STREAM ? 2 * CoreStream<N, J, LDG>::CH : (size_t)Pow<J, N - 1>::v * LDG;
   L.fn = (const void *)k_mode_spec<V, N, J, NPT, KIND, STREAM>;
+  if constexpr (KIND == kUpdate && std::is_same<V, float>::value)
+    L.fn_multi = (const void *)k_mode_spec_multi<V, N, J, NPT, KIND, STREAM>;
   L.smem = tile_smem_bytes(sizeof(V), gp, LEV, NPT, J, ldd_for(J), pairs_for(J), kThreads * NPT);
   L.tn = kThreads * NPT;
   L.spec = true;
@@ -1000,6 +1019,8 @@ template <class V, int KIND, int NPT> bool find_spec(Launch &L, const DevTensor 
 }
 
 constexpr size_t kSmemLimit = 227 * 1024;
+constexpr int kSolveMultiThreads = 64;  // batched row solves: threads per block
+constexpr int kLuMultiThreads = 128;    // batched pivoted-LU pass: 4 warps per block
 constexpr int kThreadSolveMaxJ = 24;  // larger ranks solve one row per warp
 // precision form: rows whose 1-norm condition estimate exceeds this are solved
 // in FP64 (one FP32 refinement step leaves ~(kappa * 2^-24)^2)
@@ -1581,6 +1602,485 @@ int upload_core_perms(DevTensor &t, const void *core_host) {
     GTK_CUDA(cudaMemcpyAsync(t.corep[n], buf.data(), buf.size(), cudaMemcpyHostToDevice, t.stream));
     GTK_CUDA(cudaStreamSynchronize(t.stream));
   }
+  return 0;
+}
+
+
+// ---------------------------------------------------------------- batches
+// gtk_batch_sweep's fused form: a sweep of many handles in few launches.
+
+static_assert(sizeof(ModeArgs) <= kModeArgsBytes, "the argument block must fit MultiDesc::args");
+
+// the entry i with first[i] <= k < first[i + 1] (first[0] = 0)
+__device__ __forceinline__ int slot_of64(const uint64_t *__restrict__ first, int count, uint64_t k) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= k)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+struct ZeroItem {
+  double *gram;
+  unsigned int *nfb;
+};
+// every handle's Gram/RHS rows of the level's mode (first: prefix of the doubles),
+// and its per-mode LU / FP64 list counts
+__global__ void k_batch_zero(const ZeroItem *__restrict__ items, const uint64_t *__restrict__ first, int count) {
+  const uint64_t total = first[count];
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < (uint64_t)count) items[g].nfb[0] = items[g].nfb[1] = 0u;
+  for (uint64_t k = g; k < total; k += (uint64_t)gridDim.x * blockDim.x) {
+    const int i = slot_of64(first, count, k);
+    items[i].gram[k - first[i]] = 0.0;
+  }
+}
+
+struct SolveItem {
+  const double *gram;
+  void *fac;
+  int J, E, ldf, prec32, dbl;
+  uint32_t *lu_list;     // rows for pivoted LU, count nfb[0]
+  uint32_t *fp64_list;   // precision forms: rows for FP64 Cholesky, count nfb[1]
+  unsigned int *nfb;
+  int *status;
+};
+
+// every row of every handle (first: prefix of the row counts): FP32 Cholesky +
+// estimate + refinement for the precision forms, FP64 Cholesky for the plain
+// form, each as the handle's own solve kernel does it
+__global__ void k_solve_multi(const SolveItem *__restrict__ items, const uint64_t *__restrict__ first, int count,
+                              double lambda, float cond_max) {
+  extern __shared__ __align__(16) unsigned char smb[];
+  const int T = blockDim.x, tid = threadIdx.x;
+  const uint64_t total = first[count];
+  for (uint64_t k = (uint64_t)blockIdx.x * T + tid; k < total; k += (uint64_t)gridDim.x * T) {
+    const int i = slot_of64(first, count, k);
+    const SolveItem &it = items[i];
+    const uint64_t row = k - first[i];
+    if (it.prec32) {
+      float *sf = reinterpret_cast<float *>(smb) + tid;
+      if (it.dbl)
+        solve_row32<double>(it.gram, row, it.J, it.E, it.ldf, (double *)it.fac, lambda, cond_max, sf, T, it.fp64_list,
+                            it.nfb + 1);
+      else
+        solve_row32<float>(it.gram, row, it.J, it.E, it.ldf, (float *)it.fac, lambda, cond_max, sf, T, it.fp64_list,
+                           it.nfb + 1);
+    } else {
+      double *A = reinterpret_cast<double *>(smb) + tid;
+      if (it.dbl)
+        solve_row64<double>(it.gram, row, it.J, it.E, it.ldf, (double *)it.fac, lambda, A, T, it.lu_list, it.nfb);
+      else
+        solve_row64<float>(it.gram, row, it.J, it.E, it.ldf, (float *)it.fac, lambda, A, T, it.lu_list, it.nfb);
+    }
+  }
+}
+
+// the precision forms' FP64 list of every handle: `per` CTAs per handle
+__global__ void k_solve_list64_multi(const SolveItem *__restrict__ items, int count, double lambda, int per) {
+  extern __shared__ __align__(16) unsigned char smb[];
+  const int T = blockDim.x, tid = threadIdx.x;
+  const int i = blockIdx.x / per, sub = blockIdx.x % per;
+  if (i >= count) return;
+  const SolveItem &it = items[i];
+  if (!it.prec32) return;
+  const uint64_t n = it.nfb[1];
+  double *A = reinterpret_cast<double *>(smb) + tid;
+  for (uint64_t k = (uint64_t)sub * T + tid; k < n; k += (uint64_t)per * T) {
+    if (it.dbl)
+      solve_row64<double>(it.gram, it.fp64_list[k], it.J, it.E, it.ldf, (double *)it.fac, lambda, A, T, it.lu_list,
+                          it.nfb);
+    else
+      solve_row64<float>(it.gram, it.fp64_list[k], it.J, it.E, it.ldf, (float *)it.fac, lambda, A, T, it.lu_list,
+                         it.nfb);
+  }
+}
+
+// the pivoted-LU list of every handle, one warp per row, `per` CTAs per handle
+__global__ void k_solve_lu_multi(const SolveItem *__restrict__ items, int count, double lambda, int per, int maxJ) {
+  extern __shared__ double sm[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const int i = blockIdx.x / per, sub = blockIdx.x % per;
+  if (i >= count) return;
+  const SolveItem &it = items[i];
+  const int J = it.J;
+  double *A = sm + (size_t)wib * ((size_t)maxJ * maxJ + maxJ);
+  double *b = A + (size_t)J * J;
+  const uint64_t n = it.nfb[0];
+  for (uint64_t k = (uint64_t)sub * wpb + wib; k < n; k += (uint64_t)per * wpb) {
+    const uint32_t row = it.lu_list[k];
+    load_system(it.gram + (uint64_t)row * it.E, J, it.E, lambda, A, b, lane);
+    const bool ok = lu_solve(A, b, J, lane);
+    if (lane == 0) atomicOr(it.status, ok ? 4 : 1);
+    for (int j = lane; j < it.ldf; j += 32) {
+      const double v = j < J ? b[j] : 0.0;
+      if (it.dbl)
+        ((double *)it.fac)[(uint64_t)row * it.ldf + j] = v;
+      else
+        ((float *)it.fac)[(uint64_t)row * it.ldf + j] = (float)v;
+    }
+    __syncwarp();
+  }
+}
+
+struct FitItem {
+  int use_gram, dbl;
+  const double *gram;  // use_gram: the last mode's Gram/RHS rows
+  const void *fac;     // the last mode's factor
+  uint64_t rows;
+  int J, E, ldf;
+  double normsq;
+  const void *dstore;    // else: the last mode's stored delta (view order)
+  const uint32_t *row_of;
+  const void *val;
+  uint64_t nnz;
+  double *partial;
+  int *status;
+};
+
+template <class V> __device__ double fit_gram_part(const FitItem &f, uint64_t c, uint64_t nc) {
+  double s = 0;
+  const V *fac = (const V *)f.fac;
+  for (uint64_t r = c * blockDim.x + threadIdx.x; r < f.rows; r += nc * blockDim.x) {
+    const double *g = f.gram + r * (uint64_t)f.E;
+    const V *a = fac + r * (uint64_t)f.ldf;
+    double q = 0;
+    int e = 0;
+    for (int i = 0; i < f.J; ++i) {
+      const double ai = (double)a[i];
+      double t = 0.5 * g[e++] * ai;
+      for (int j = i + 1; j < f.J; ++j) t += g[e++] * (double)a[j];
+      q += ai * (2.0 * g[e++] - 2.0 * t);
+    }
+    s += q;
+  }
+  return s;
+}
+template <class V> __device__ double fit_stored_part(const FitItem &f, uint64_t c, uint64_t nc) {
+  double err = 0;
+  const V *d0 = (const V *)f.dstore, *fac = (const V *)f.fac, *val = (const V *)f.val;
+  for (uint64_t t = c * blockDim.x + threadIdx.x; t < f.nnz; t += nc * blockDim.x) {
+    const V *d = d0 + t * (uint64_t)f.J;
+    const V *a = fac + (uint64_t)f.row_of[t] * f.ldf;
+    V xh = V(0);
+    for (int j = 0; j < f.J; ++j) xh += d[j] * a[j];
+    const V e = val[t] - xh;
+    err += (double)e * (double)e;
+  }
+  return err;
+}
+
+// every handle's fit partial sums (as k_fit_gram / k_fit_stored), CTA ranges per handle
+__global__ void __launch_bounds__(256)
+    k_fit_multi(const FitItem *__restrict__ items, const uint32_t *__restrict__ cta_first, int count) {
+  const int i = slot_of(cta_first, count, blockIdx.x);
+  const FitItem &f = items[i];
+  const uint64_t c = blockIdx.x - cta_first[i], nc = cta_first[i + 1] - cta_first[i];
+  double v;
+  if (f.use_gram)
+    v = f.dbl ? fit_gram_part<double>(f, c, nc) : fit_gram_part<float>(f, c, nc);
+  else
+    v = f.dbl ? fit_stored_part<double>(f, c, nc) : fit_stored_part<float>(f, c, nc);
+  const double tot = block_sum(v);
+  if (threadIdx.x == 0) f.partial[c] = f.use_gram ? (c == 0 ? f.normsq : 0.0) - tot : tot;
+}
+
+// per handle: the error sum (also into its own sum slot) and its status word, cleared
+__global__ void k_fit_sum_multi(const FitItem *__restrict__ items, const uint32_t *__restrict__ cta_first, int count,
+                                double *__restrict__ err_out, int *__restrict__ st_out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  const FitItem &f = items[i];
+  double s = 0;
+  for (uint32_t c = 0; c < cta_first[i + 1] - cta_first[i]; ++c) s += f.partial[c];
+  f.partial[kFitSumSlot] = s;
+  err_out[i] = s;
+  const int st = *f.status;
+  st_out[i] = st;
+  if (st) *f.status = 0;
+}
+
+template <class V> static int spec_multi_desc(DevTensor &t, int mode, MultiDesc *d) {
+  Launch L;
+  bool gp = true;
+  choose<V, kUpdate>(L, t, gp);
+  if (!L.spec || !L.fn_multi || L.smem > kSmemLimit) return GTK_ERR_UNSUPPORTED;
+  if (int rc = prepare_fn(L.fn_multi, L.smem)) return rc;
+  ModeArgs a = make_args(t, mode);
+  a.gp_in_smem = gp ? 1 : 0;
+  a.ref_order = 0;
+  a.core = t.core;
+  a.dstore = mode == t.N - 1 ? t.dstore : nullptr;  // the plain form's fit reads the last mode's delta
+  int per_sm = 0;
+  GTK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn_multi, kThreads, L.smem));
+  if (per_sm < 1) return fail(GTK_ERR_UNSUPPORTED, "mode kernel does not fit on an SM");
+  const uint64_t ntiles = (a.nnz + L.tn - 1) / L.tn;
+  d->fn = L.fn_multi;
+  d->threads = kThreads;
+  d->smem = L.smem;
+  d->ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)per_sm * t.num_sms));
+  d->with_image = false;
+  d->image = nullptr;
+  memcpy(d->args, &a, sizeof(a));
+  return 0;
+}
+
+struct FusedBatch {
+  struct Group {  // one kernel class of one level
+    MultiDesc proto;
+    int count = 0;
+    uint32_t grid = 0;
+    size_t args_off = 0, first_off = 0, img_off = 0;  // offsets into dev
+  };
+  struct Level {
+    int count = 0;  // handles with a mode of this index
+    size_t zero_off = 0, zfirst_off = 0, solve_off = 0, sfirst_off = 0;
+    uint64_t zero_total = 0, rows_total = 0;
+    bool any32 = false;
+    int maxJ = 1;
+    size_t solve_smem = 0, list_smem = 0, lu_smem = 0;
+    std::vector<Group> groups;
+  };
+  std::vector<Level> levels;
+  int count = 0;
+  size_t fit_off = 0, ffirst_off = 0;
+  uint32_t fit_grid = 0;
+  unsigned char *dev = nullptr;
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> ev;  // fork per level, then joins per (level, group)
+  int dev_id = 0;
+};
+
+void fused_batch_free(FusedBatch *fb) {
+  if (!fb) return;
+  for (cudaStream_t s : fb->side)
+    if (s) cudaStreamDestroy(s);
+  for (cudaEvent_t e : fb->ev)
+    if (e) cudaEventDestroy(e);
+  if (fb->dev) cudaFree(fb->dev);
+  delete fb;
+}
+
+int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
+  *out = nullptr;
+  int maxN = 0;
+  for (DevTensor *t : ts) {
+    if (t->streamed || t->variant == kVarRefOrder || t->J > kThreadSolveMaxJ || !t->nnz) return GTK_ERR_UNSUPPORTED;
+    if (!tc_update(*t) && t->dtype != GTK_F32) return GTK_ERR_UNSUPPORTED;
+    if (!tc_update(*t)) {
+      if (int rc = ensure_dstore(*t)) return rc;
+      if (!t->dstore) return GTK_ERR_UNSUPPORTED;
+    }
+    maxN = std::max(maxN, t->N);
+  }
+  std::unique_ptr<FusedBatch, void (*)(FusedBatch *)> fb(new FusedBatch(), fused_batch_free);
+  fb->count = (int)ts.size();
+  GTK_CUDA(cudaGetDevice(&fb->dev_id));
+  std::vector<unsigned char> host;  // the device tables, 16-byte aligned pieces
+  auto put = [&](const void *p, size_t n) {
+    const size_t off = (host.size() + 15) / 16 * 16;
+    host.resize(off + n);
+    memcpy(host.data() + off, p, n);
+    return off;
+  };
+  for (int n = 0; n < maxN; ++n) {
+    FusedBatch::Level L;
+    std::vector<ZeroItem> zi;
+    std::vector<uint64_t> zf(1, 0);
+    std::vector<SolveItem> si;
+    std::vector<uint64_t> sf(1, 0);
+    size_t max_e64 = 0, max_e32 = 0;
+    std::vector<std::pair<MultiDesc, DevTensor *>> descs;
+    for (DevTensor *t : ts) {
+      if (n >= t->N) continue;
+      MultiDesc d;
+      int rc = tc_update(*t) ? tc_multi_desc(*t, n, &d) : spec_multi_desc<float>(*t, n, &d);
+      if (rc) return rc;
+      descs.emplace_back(d, t);
+      const int E = pairs_for(t->J);
+      zi.push_back({t->gram, t->nfallback});
+      zf.push_back(zf.back() + t->rows[n] * (uint64_t)E);
+      SolveItem s;
+      s.gram = t->gram;
+      s.fac = t->fac[n];
+      s.J = t->J;
+      s.E = E;
+      s.ldf = t->ldf;
+      s.prec32 = t->precision != GTK_PREC_PLAIN ? 1 : 0;
+      s.dbl = t->dtype == GTK_F64 ? 1 : 0;
+      s.lu_list = t->fallback;
+      s.fp64_list = t->fallback64;
+      s.nfb = t->nfallback;
+      s.status = t->status;
+      si.push_back(s);
+      sf.push_back(sf.back() + t->rows[n]);
+      max_e64 = std::max<size_t>(max_e64, (size_t)E * 8);
+      if (s.prec32) max_e32 = std::max<size_t>(max_e32, (size_t)(E + 3 * t->J) * 4);
+      L.any32 = L.any32 || s.prec32;
+      L.maxJ = std::max(L.maxJ, t->J);
+    }
+    L.count = (int)si.size();
+    L.zero_total = zf.back();
+    L.rows_total = sf.back();
+    L.zero_off = put(zi.data(), zi.size() * sizeof(ZeroItem));
+    L.zfirst_off = put(zf.data(), zf.size() * 8);
+    L.solve_off = put(si.data(), si.size() * sizeof(SolveItem));
+    L.sfirst_off = put(sf.data(), sf.size() * 8);
+    L.solve_smem = kSolveMultiThreads * std::max(max_e64, max_e32);
+    L.list_smem = kSolveMultiThreads * max_e64;
+    L.lu_smem = (size_t)(kLuMultiThreads / 32) * ((size_t)L.maxJ * L.maxJ + L.maxJ) * 8;
+    // kernel classes: the same multi-tensor kernel, shared memory and block
+    for (auto &pd : descs) {
+      const MultiDesc &d = pd.first;
+      FusedBatch::Group *g = nullptr;
+      for (auto &x : L.groups)
+        if (x.proto.fn == d.fn && x.proto.smem == d.smem && x.proto.threads == d.threads) g = &x;
+      if (!g) {
+        L.groups.emplace_back();
+        g = &L.groups.back();
+        g->proto = d;
+      }
+      g->count += 1;
+    }
+    for (auto &g : L.groups) {
+      std::vector<unsigned char> args;
+      std::vector<uint32_t> first(1, 0);
+      std::vector<const unsigned char *> imgs;
+      for (auto &pd : descs) {
+        const MultiDesc &d = pd.first;
+        if (d.fn != g.proto.fn || d.smem != g.proto.smem || d.threads != g.proto.threads) continue;
+        args.insert(args.end(), d.args, d.args + kModeArgsBytes);
+        first.push_back(first.back() + d.ctas);
+        imgs.push_back(d.image);
+      }
+      g.grid = first.back();
+      g.args_off = put(args.data(), args.size());
+      g.first_off = put(first.data(), first.size() * 4);
+      g.img_off = put(imgs.data(), imgs.size() * sizeof(void *));
+    }
+    fb->levels.push_back(std::move(L));
+  }
+  // the fit: each handle's last mode
+  {
+    std::vector<FitItem> fi;
+    std::vector<uint32_t> ff(1, 0);
+    for (DevTensor *t : ts) {
+      const int m = t->N - 1;
+      FitItem f;
+      memset(&f, 0, sizeof(f));
+      f.use_gram = tc_update(*t) ? 1 : 0;
+      f.dbl = t->dtype == GTK_F64 ? 1 : 0;
+      f.gram = t->gram;
+      f.fac = t->fac[m];
+      f.rows = t->rows[m];
+      f.J = t->J;
+      f.E = pairs_for(t->J);
+      f.ldf = t->ldf;
+      f.normsq = t->norm * t->norm;
+      f.dstore = t->dstore;
+      f.row_of = t->vidx[m][m];
+      f.val = t->vval[m];
+      f.nnz = t->nnz;
+      f.partial = t->partial;
+      f.status = t->status;
+      const uint64_t work = f.use_gram ? f.rows : f.nnz;
+      const uint32_t ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(kFitGridMax, (work + 255) / 256));
+      fi.push_back(f);
+      ff.push_back(ff.back() + ctas);
+    }
+    fb->fit_grid = ff.back();
+    fb->fit_off = put(fi.data(), fi.size() * sizeof(FitItem));
+    fb->ffirst_off = put(ff.data(), ff.size() * 4);
+  }
+  GTK_CUDA(malloc_retry(&fb->dev, std::max<size_t>(host.size(), 16)));
+  GTK_CUDA(cudaMemcpy(fb->dev, host.data(), host.size(), cudaMemcpyHostToDevice));
+  size_t groups = 0;
+  for (auto &L : fb->levels) groups = std::max(groups, L.groups.size());
+  const size_t nside = std::min<size_t>(groups, 4);
+  fb->side.assign(nside, nullptr);
+  for (auto &s : fb->side) GTK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  size_t nev = 0;
+  for (auto &L : fb->levels) nev += 1 + L.groups.size();
+  fb->ev.assign(nev, nullptr);
+  for (auto &e : fb->ev) GTK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  for (auto &L : fb->levels) {
+    if (int rc = prepare_fn((const void *)k_solve_multi, L.solve_smem)) return rc;
+    if (int rc = prepare_fn((const void *)k_solve_list64_multi, L.list_smem)) return rc;
+    if (int rc = prepare_fn((const void *)k_solve_lu_multi, L.lu_smem)) return rc;
+  }
+  *out = fb.release();
+  return 0;
+}
+
+int fused_batch_enqueue(FusedBatch *fb, cudaStream_t s, double *err_out, int *status_out, uint64_t *kernels) {
+  uint64_t k = 0;
+  size_t ev = 0;
+  unsigned char *D = fb->dev;
+  for (auto &L : fb->levels) {
+    const int n = L.count;
+    {
+      const uint64_t blocks = std::max<uint64_t>((L.zero_total + 255) / 256, (uint64_t)(n + 255) / 256);
+      k_batch_zero<<<(unsigned)std::min<uint64_t>(blocks, 8192), 256, 0, s>>>(
+          (const ZeroItem *)(D + L.zero_off), (const uint64_t *)(D + L.zfirst_off), n);
+      GTK_CUDA(cudaGetLastError());
+      ++k;
+    }
+    // the update launches, one per kernel class, on side streams
+    cudaEvent_t fork = fb->ev[ev++];
+    GTK_CUDA(cudaEventRecord(fork, s));
+    for (size_t gi = 0; gi < L.groups.size(); ++gi) {
+      const FusedBatch::Group &g = L.groups[gi];
+      // classes that allocate tensor memory run one after another on the main
+      // stream (each kernel's residency limit keeps its CTAs within an SM's 512
+      // columns; two such kernels side by side could exceed it); the SIMT
+      // classes run beside them on side streams
+      cudaStream_t cs = (fb->side.empty() || g.proto.tmem) ? s : fb->side[gi % fb->side.size()];
+      GTK_CUDA(cudaStreamWaitEvent(cs, fork, 0));
+      const void *args = D + g.args_off;
+      const void *first = D + g.first_off;
+      const void *imgs = D + g.img_off;
+      int cnt = g.count;
+      if (g.proto.with_image) {
+        void *p[] = {&args, &imgs, &first, &cnt};
+        GTK_CUDA(cudaLaunchKernel(g.proto.fn, dim3(g.grid), dim3(g.proto.threads), p, g.proto.smem, cs));
+      } else {
+        void *p[] = {&args, &first, &cnt};
+        GTK_CUDA(cudaLaunchKernel(g.proto.fn, dim3(g.grid), dim3(g.proto.threads), p, g.proto.smem, cs));
+      }
+      cudaEvent_t join = fb->ev[ev++];
+      if (cs != s) {
+        GTK_CUDA(cudaEventRecord(join, cs));
+        GTK_CUDA(cudaStreamWaitEvent(s, join, 0));
+      }
+      ++k;
+    }
+    const SolveItem *si = (const SolveItem *)(D + L.solve_off);
+    const uint64_t *sfirst = (const uint64_t *)(D + L.sfirst_off);
+    const unsigned sg = (unsigned)std::max<uint64_t>(
+        1, std::min<uint64_t>((L.rows_total + kSolveMultiThreads - 1) / kSolveMultiThreads, 65535));
+    k_solve_multi<<<sg, kSolveMultiThreads, L.solve_smem, s>>>(si, sfirst, n, kLambda, kCondMaxFp32);
+    GTK_CUDA(cudaGetLastError());
+    ++k;
+    if (L.any32) {
+      k_solve_list64_multi<<<(unsigned)(n * 2), kSolveMultiThreads, L.list_smem, s>>>(si, n, kLambda, 2);
+      GTK_CUDA(cudaGetLastError());
+      ++k;
+    }
+    k_solve_lu_multi<<<(unsigned)(n * 2), kLuMultiThreads, L.lu_smem, s>>>(si, n, kLambda, 2, L.maxJ);
+    GTK_CUDA(cudaGetLastError());
+    ++k;
+  }
+  const FitItem *fi = (const FitItem *)(D + fb->fit_off);
+  const uint32_t *ff = (const uint32_t *)(D + fb->ffirst_off);
+  k_fit_multi<<<fb->fit_grid, 256, 0, s>>>(fi, ff, fb->count);
+  k_fit_sum_multi<<<(fb->count + 127) / 128, 128, 0, s>>>(fi, ff, fb->count, err_out, status_out);
+  GTK_CUDA(cudaGetLastError());
+  k += 2;
+  if (kernels) *kernels = k;
   return 0;
 }
 

@@ -377,6 +377,7 @@ __global__ void __launch_bounds__(kTsThreads, 1)
 
 struct TsLaunch {
   const void *fn = nullptr;
+  const void *fn_multi = nullptr;  // the multi-tensor form (updates), for batches
   void (*build)(const float *, int, unsigned char *, cudaStream_t) = nullptr;
   int smem = 0, ncols = 0;
   size_t img_bytes = 0;
@@ -392,6 +393,7 @@ template <int N, int J, int KIND> TsLaunch ts_entry() {
   using S = TsShape<N, J>;
   TsLaunch L;
   L.fn = (const void *)k_mode_tcs<N, J, KIND>;
+  if constexpr (KIND == 0) L.fn_multi = (const void *)k_mode_tcs_multi<N, J, KIND>;
   L.build = build_img<N, J>;
   L.smem = S::SMEM;
   L.ncols = 2 * S::NCOLS;
@@ -449,6 +451,51 @@ int ts_prepare(const TsLaunch &L, int num_sms, int *grid_cap, int *smem_out) {
 }
 
 }  // namespace
+
+// a handle's mode update as one entry of its class's multi-tensor launch (batches)
+int ts_multi_desc(DevTensor &t, int mode, MultiDesc *d) {
+  TsLaunch L;
+  if (t.dtype != GTK_F32 || t.precision != GTK_PREC_BF16 || !ts_choose(L, 0, t.N, t.J) || !L.fn_multi)
+    return GTK_ERR_UNSUPPORTED;
+  if (!t.bimg[mode]) return fail(GTK_ERR_STATE, "core image missing (set the precision after the core)");
+  TsLaunch M = L;
+  M.fn = L.fn_multi;
+  int cap = 0, smem = 0;
+  if (int rc = ts_prepare(M, t.num_sms, &cap, &smem)) return rc;
+  ModeArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int k = 0; k < t.N; ++k) {
+    a.coord[k] = t.vidx[mode][k];
+    a.fac[k] = t.fac[k];
+  }
+  a.val = t.vval[mode];
+  a.corep = t.corep[mode];
+  a.vperm = t.vperm[mode];
+  a.gram = t.gram;
+  a.partial = t.partial;
+  a.status = t.status;
+  a.nnz = t.nnz;
+  a.N = t.N;
+  a.J = t.J;
+  a.ldf = t.ldf;
+  a.mode = mode;
+  a.E = pairs_for(t.J);
+  a.ldd = ldd_for(t.J);
+  int m = 0;
+  for (int k = 0; k < t.N; ++k)
+    if (k != mode) a.others[m++] = k;
+  const uint64_t ntiles = (t.nnz + kTsThreads - 1) / kTsThreads;
+  d->fn = L.fn_multi;
+  d->threads = kTsThreads;
+  d->smem = (size_t)smem;
+  d->ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)cap));
+  d->with_image = true;
+  d->image = t.bimg[mode];
+  d->tmem = true;
+  static_assert(sizeof(ModeArgs) <= kModeArgsBytes, "argument block");
+  memcpy(d->args, &a, sizeof(a));
+  return 0;
+}
 
 bool ts_supported(int N, int J, int dtype, int prec) {
   TsLaunch L;

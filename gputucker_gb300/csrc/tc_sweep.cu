@@ -363,6 +363,7 @@ __global__ void __launch_bounds__(kTcThreads)
 
 struct TcLaunch {
   const void *fn = nullptr;
+  const void *fn_multi = nullptr;  // the multi-tensor form (updates), for batches
   int smem = 0, ncols = 0;
 };
 
@@ -370,6 +371,7 @@ template <int J, int D, int PREC, int KIND> TcLaunch tc_entry() {
   using S = TcShape<J, D, PREC>;
   TcLaunch L;
   L.fn = (const void *)k_mode_tc<J, D, PREC, KIND>;
+  if constexpr (KIND == 0) L.fn_multi = (const void *)k_mode_tc_multi<J, D, PREC, KIND>;
   L.smem = S::SMEM;
   L.ncols = S::NCOLS;
   return L;
@@ -439,6 +441,53 @@ int tc_prepare_uncached(const TcLaunch &L, int num_sms, int *grid_cap, int *smem
 }
 
 }  // namespace
+
+// a handle's mode update as one entry of its class's multi-tensor launch (batches)
+int tc_multi_desc(DevTensor &t, int mode, MultiDesc *d) {
+  TcLaunch L;
+  if (!tc_choose<0>(L, t.precision, t.N, t.J)) {
+    if (ts_supported(t.N, t.J, t.dtype, t.precision)) return ts_multi_desc(t, mode, d);
+    return GTK_ERR_UNSUPPORTED;
+  }
+  if (t.dtype != GTK_F32 || !L.fn_multi) return GTK_ERR_UNSUPPORTED;
+  TcLaunch M = L;
+  M.fn = L.fn_multi;  // attributes and residency of the multi-tensor kernel itself
+  int cap = 0, smem = 0;
+  if (int rc = tc_prepare(M, t.num_sms, &cap, &smem)) return rc;
+  ModeArgs a;
+  memset(&a, 0, sizeof(a));
+  for (int k = 0; k < t.N; ++k) {
+    a.coord[k] = t.vidx[mode][k];
+    a.fac[k] = t.fac[k];
+  }
+  a.val = t.vval[mode];
+  a.corep = t.corep[mode];
+  a.vperm = t.vperm[mode];
+  a.gram = t.gram;
+  a.partial = t.partial;
+  a.status = t.status;
+  a.nnz = t.nnz;
+  a.N = t.N;
+  a.J = t.J;
+  a.ldf = t.ldf;
+  a.mode = mode;
+  a.E = pairs_for(t.J);
+  a.ldd = ldd_for(t.J);
+  int m = 0;
+  for (int k = 0; k < t.N; ++k)
+    if (k != mode) a.others[m++] = k;
+  const uint64_t ntiles = (t.nnz + kTcThreads - 1) / kTcThreads;
+  d->fn = L.fn_multi;
+  d->threads = kTcThreads;
+  d->smem = (size_t)smem;
+  d->ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)cap));
+  d->with_image = false;
+  d->image = nullptr;
+  d->tmem = true;
+  static_assert(sizeof(ModeArgs) <= kModeArgsBytes, "argument block");
+  memcpy(d->args, &a, sizeof(a));
+  return 0;
+}
 
 bool tc_supported(int N, int J, int dtype, int prec) {
   if (dtype != GTK_F32 || (prec != GTK_PREC_BF16 && prec != GTK_PREC_TF32)) return false;

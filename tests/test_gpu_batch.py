@@ -220,3 +220,74 @@ def test_streamed_core_kernels(N, J):
     finally:
         for t in ts.values():
             t.close()
+
+
+# FP32 handles of every kernel family: SIMT (orders 3-5), tcgen05 BF16/TF32, the
+# streamed-core tcgen05 form (order 5; order 4 at rank 16)
+FUSED = [
+    ([30, 25, 28, 20], [2, 1, 2, 1], 10, 20000, np.float32, "plain"),
+    ([40, 35, 30], [1, 2, 1], 8, 12000, np.float32, "bf16"),
+    ([50, 40, 45, 30], [1, 1, 1, 2], 8, 30000, np.float32, "tf32"),
+    ([16, 12, 14, 10, 9], [1, 1, 1, 1, 1], 4, 5000, np.float32, "plain"),
+    ([14, 12, 13, 11, 10], [1, 1, 1, 1, 1], 8, 8000, np.float32, "bf16"),
+    ([30, 28, 26, 24], [1, 1, 1, 1], 16, 20000, np.float32, "bf16"),
+    ([60, 50, 40], [2, 1, 1], 12, 15000, np.float32, "plain"),
+    ([45, 40, 35], [1, 1, 1], 4, 9000, np.float32, "plain"),
+]
+
+
+def test_fused_batch_few_launches_match_one_by_one_and_oracle(monkeypatch):
+    """The fused sweep (per mode index: one zeroing kernel, one launch per update
+    kernel class, the batched row solves; one fit and one reduction) against the
+    same handles swept one by one, against the per-handle graph
+    (GTK_BATCH_FUSED=0), and three members against the FP64 oracle."""
+    from oracle_util import Oracle
+    pairs = [_make(c, 200 + i) for i, c in enumerate(FUSED)]
+    batch_ts = [p[0] for p in pairs]
+    solo_ts = [p[1] for p in pairs]
+    try:
+        with gtk.Batch(batch_ts) as b:
+            for sweep in range(3):
+                fb = b.sweep()
+                fs = [t.sweep() for t in solo_ts]
+                assert np.all(np.abs(fb - np.array(fs)) <= 1e-6), (sweep, fb, fs)
+            k_fused = b.kernels()
+            maxN = max(len(c[0]) for c in FUSED)
+            classes = len({(len(c[0]), c[2], c[5]) for c in FUSED})
+            # per mode index: zeroing + at most one launch per class + 3 solve passes; fit + reduction
+            assert 0 < k_fused <= maxN * (1 + classes + 3) + 2, k_fused
+            for i, c in enumerate(FUSED):
+                for n in range(len(c[0])):
+                    assert rel_fro(batch_ts[i].get_factor(n), solo_ts[i].get_factor(n)) <= 1e-4, (i, n)
+        # the per-handle graph gives the same sweep with one launch chain per handle
+        monkeypatch.setenv("GTK_BATCH_FUSED", "0")
+        for t in batch_ts:
+            t.init_random(1, 0)
+        with gtk.Batch(batch_ts) as b2:
+            f2 = [b2.sweep() for _ in range(2)][-1]
+            assert b2.kernels() > 4 * k_fused
+        for t in batch_ts:
+            t.init_random(1, 0)
+        monkeypatch.delenv("GTK_BATCH_FUSED")
+        with gtk.Batch(batch_ts) as b3:
+            f3 = [b3.sweep() for _ in range(2)][-1]
+        assert np.all(np.abs(f3 - f2) <= 1e-6), (f3, f2)
+        # three members against the FP64 oracle after 3 fused sweeps of the same data
+        # and initialisation: plain FP32 within the FP32 bound, BF16 / TF32 within theirs
+        for t in batch_ts:
+            t.init_random(1, 0)
+        with gtk.Batch(batch_ts) as b4:
+            f4 = [b4.sweep() for _ in range(3)][-1]
+        for i, tol in ((0, 1e-4), (1, 1e-3), (2, 2e-4)):
+            dims, P, J, nnz, dtype, prec = FUSED[i]
+            rng = np.random.default_rng(200 + i)
+            idx = random_coo(rng, dims, nnz)
+            vals = rng.random(len(idx[0])).astype(dtype)
+            ora = Oracle(1, idx, vals.astype(np.float64), dims, P, J)
+            ora.init_random(1, 0)
+            fo = [ora.sweep()["fit64"] for _ in range(3)][-1]
+            assert abs(f4[i] - fo) <= tol, (i, prec, f4[i], fo)
+    finally:
+        for p in pairs:
+            for t in p:
+                t.close()
