@@ -1953,7 +1953,7 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
       for (auto &pd : descs) {
         const MultiDesc &d = pd.first;
         if (d.fn != g.proto.fn || d.smem != g.proto.smem || d.threads != g.proto.threads) continue;
-        args.insert(args.end(), d.args, d.args + kModeArgsBytes);
+        args.insert(args.end(), d.args, d.args + sizeof(ModeArgs));  // the kernels index a ModeArgs array
         first.push_back(first.back() + d.ctas);
         imgs.push_back(d.image);
       }
