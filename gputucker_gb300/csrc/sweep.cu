@@ -1662,14 +1662,17 @@ __global__ void k_solve_multi(const SolveItem *__restrict__ items, const uint64_
     const int i = slot_of64(first, count, k);
     const SolveItem &it = items[i];
     const uint64_t row = k - first[i];
+    // every thread's scratch in 8-byte slots (element e at slot e * T + tid) for
+    // both paths: threads of one block may solve rows of an FP32-path and of an
+    // FP64-path handle at once, and interleaving 4- and 8-byte elements would overlap
     if (it.prec32) {
-      float *sf = reinterpret_cast<float *>(smb) + tid;
+      float *sf = reinterpret_cast<float *>(smb) + 2 * tid;
       if (it.dbl)
-        solve_row32<double>(it.gram, row, it.J, it.E, it.ldf, (double *)it.fac, lambda, cond_max, sf, T, it.fp64_list,
-                            it.nfb + 1);
+        solve_row32<double>(it.gram, row, it.J, it.E, it.ldf, (double *)it.fac, lambda, cond_max, sf, 2 * T,
+                            it.fp64_list, it.nfb + 1);
       else
-        solve_row32<float>(it.gram, row, it.J, it.E, it.ldf, (float *)it.fac, lambda, cond_max, sf, T, it.fp64_list,
-                           it.nfb + 1);
+        solve_row32<float>(it.gram, row, it.J, it.E, it.ldf, (float *)it.fac, lambda, cond_max, sf, 2 * T,
+                           it.fp64_list, it.nfb + 1);
     } else {
       double *A = reinterpret_cast<double *>(smb) + tid;
       if (it.dbl)
@@ -1919,7 +1922,7 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
       si.push_back(s);
       sf.push_back(sf.back() + t->rows[n]);
       max_e64 = std::max<size_t>(max_e64, (size_t)E * 8);
-      if (s.prec32) max_e32 = std::max<size_t>(max_e32, (size_t)(E + 3 * t->J) * 4);
+      if (s.prec32) max_e32 = std::max<size_t>(max_e32, (size_t)(E + 3 * t->J) * 8);  // 8-byte slots
       L.any32 = L.any32 || s.prec32;
       L.maxJ = std::max(L.maxJ, t->J);
     }
