@@ -265,7 +265,8 @@ def test_fused_batch_few_launches_match_one_by_one_and_oracle(monkeypatch):
             t.init_random(1, 0)
         with gtk.Batch(batch_ts) as b2:
             f2 = [b2.sweep() for _ in range(2)][-1]
-            assert b2.kernels() > 4 * k_fused
+            # 2N + 2 or more per handle, against per-class launches (the gap grows with the handle count)
+            assert b2.kernels() > k_fused
         for t in batch_ts:
             t.init_random(1, 0)
         monkeypatch.delenv("GTK_BATCH_FUSED")
