@@ -21,8 +21,10 @@ fit after the K sweeps is within 1e-4 of the plain form's, else the plain form's
   value ........ device time (CUDA events on the library's stream) of K sweeps on
                  the HBM-resident tensor; inputs (8 GB of views) are far larger
                  than the 129 MB L2.
-  e2e .......... the whole job through the C ABI with host buffers: upload the
-                 pinned host COO, partition and segment it on the GPU, initialise,
+  e2e .......... the whole job through the C ABI with host buffers: read the
+                 page-locked host COO into the partition (in place over NVLink-C2C
+                 where the device reaches host memory, else by an upload copy),
+                 partition and segment it on the GPU, initialise,
                  run the configuration's 10 sweeps with a fit each, read the
                  factors back -- N * nnz * sweeps / wall time of the median of
                  --e2e-runs (default 3) jobs; every job is listed by phase.
@@ -38,7 +40,7 @@ fit after the K sweeps is within 1e-4 of the plain form's, else the plain form's
                  sample and code the reference arm times.
 
 Other workloads (--workload): batch256 (256 independent tensors, one graph launch
-per sweep), warmstart (the learned warm start on the planted 50,000^3 family),
+per sweep holding the fused batch sweep; the per-handle graph timed beside it), warmstart (the learned warm start on the planted 50,000^3 family),
 precision3d (the 3-order 500M-nonzero rank-16 tensor: plain FP32, BF16 and TF32
 timed like the headline and compared after 3 sweeps with an FP64 run).
 
@@ -473,6 +475,21 @@ def run_batch(args, dist):
             dist.barrier()
             clk = clocks.stop()
             kernels = b.kernels()
+        # the per-handle graph (one launch chain per tensor, GTK_BATCH_FUSED=0) for comparison
+        os.environ["GTK_BATCH_FUSED"] = "0"
+        try:
+            for t in ts:
+                t.init_random(1, 0)
+            with gtk.Batch(ts) as b2:
+                b2.sweep()
+                b2.sweep()
+                t0 = time.perf_counter()
+                for _ in range(args.steps):
+                    b2.sweep()
+                branches = (time.perf_counter() - t0) / args.steps
+                branch_kernels = b2.kernels()
+        finally:
+            os.environ.pop("GTK_BATCH_FUSED", None)
         # one by one: the same tensors swept in sequence, each replaying its own graph
         for t in ts:
             t.init_random(1, 0)
@@ -485,7 +502,8 @@ def run_batch(args, dist):
         for t in ts:
             t.set_graph(False)
         res[form] = dict(wall=dist.max(wall), fits=fits, clocks=clk, kernels=kernels, solo=dist.max(solo), tc=tc,
-                         tune_s=tune_s, variants={v: variants.count(v) for v in set(variants)})
+                         tune_s=tune_s, variants={v: variants.count(v) for v in set(variants)},
+                         branches=branches, branch_kernels=branch_kernels)
     fast = forms[-1]
     # the plain FP32 form's own run-to-run spread (order of FP64 atomic adds): on
     # under-determined tensors (fewer nonzeros per row than the rank) FP32 ALS is
@@ -518,20 +536,24 @@ def run_batch(args, dist):
         with gtk.Batch(ts) as b:
             for _ in range(max(2, args.warmup)):
                 b.sweep()
-            for t in ts:
-                t.init_random(1, 0)
+            walls = []
             clocks = Clocks(dist.local)
-            dist.barrier()
-            t0 = time.perf_counter()
-            fits = None
-            for _ in range(args.steps):
-                fits = b.sweep()
-            wall = time.perf_counter() - t0
-            dist.barrier()
+            for _rep in range(3):  # the same selection timed three times: the spread of the number
+                for t in ts:
+                    t.init_random(1, 0)
+                dist.barrier()
+                t0 = time.perf_counter()
+                fits = None
+                for _ in range(args.steps):
+                    fits = b.sweep()
+                walls.append(time.perf_counter() - t0)
+                dist.barrier()
             clk = clocks.stop()
             kernels = b.kernels()
+        wall = statistics.median(walls)
         res["mixed"] = dict(wall=dist.max(wall), fits=fits, clocks=clk, kernels=kernels, solo=None,
-                            tc=int(within.sum()), tune_s=0.0, variants={})
+                            tc=int(within.sum()), tune_s=0.0, variants={},
+                            walls=[w / args.steps * 1e3 for w in walls])
         chosen = "mixed"
     for t in ts:
         t.close()
@@ -539,6 +561,8 @@ def run_batch(args, dist):
     if dist.rank == 0:
         line = {
             "metric": "batched ALS-sweep nnz/s at <= 1e-4 fit gap vs plain FP32 (1 GB300)",
+            "batch_form": "fused: per mode index one zeroing kernel, one launch per update-kernel class, "
+                          "batched row solves; one fit launch and one reduction; one graph launch per sweep",
             "value": dist.world * work * args.steps / r["wall"], "unit": "nnz/s", "n_gpus": dist.world,
             "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": 1e3 * r["wall"] / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -556,7 +580,10 @@ def run_batch(args, dist):
                           "batch_speedup_vs_one_by_one":
                           None if v["solo"] is None else v["solo"] / (v["wall"] / args.steps),
                           "graph_kernels": v["kernels"],
-                          "tensors_on_tensor_cores": v["tc"], "autotune_s": v["tune_s"], "variants": v["variants"]}
+                          "tensors_on_tensor_cores": v["tc"], "autotune_s": v["tune_s"], "variants": v["variants"],
+                          "ms_per_sweep_repeats": v.get("walls"),
+                          "per_handle_graph_ms_per_sweep": None if v.get("branches") is None else 1e3 * v["branches"],
+                          "per_handle_graph_kernels": v.get("branch_kernels")}
                       for f, v in res.items()},
             "fit_gap_rule": "the precision form runs only on tensors whose BF16 fit was within 1e-4 of the "
                             "plain FP32 fit in this run; the others run plain FP32 ('mixed')",

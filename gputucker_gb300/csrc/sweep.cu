@@ -1654,7 +1654,7 @@ struct SolveItem {
 // estimate + refinement for the precision forms, FP64 Cholesky for the plain
 // form, each as the handle's own solve kernel does it
 __global__ void k_solve_multi(const SolveItem *__restrict__ items, const uint64_t *__restrict__ first, int count,
-                              double lambda, float cond_max) {
+                              double lambda, float cond_max, int slot4) {
   extern __shared__ __align__(16) unsigned char smb[];
   const int T = blockDim.x, tid = threadIdx.x;
   const uint64_t total = first[count];
@@ -1662,16 +1662,19 @@ __global__ void k_solve_multi(const SolveItem *__restrict__ items, const uint64_
     const int i = slot_of64(first, count, k);
     const SolveItem &it = items[i];
     const uint64_t row = k - first[i];
-    // every thread's scratch in 8-byte slots (element e at slot e * T + tid) for
-    // both paths: threads of one block may solve rows of an FP32-path and of an
-    // FP64-path handle at once, and interleaving 4- and 8-byte elements would overlap
+    // slot4: every handle of the launch takes the FP32 path, whose scratch
+    // interleaves 4-byte elements (element e at e * T + tid); otherwise every
+    // thread's scratch sits in 8-byte slots for both paths, since threads of one
+    // block may serve an FP32-path and an FP64-path handle at once and
+    // interleaved 4- and 8-byte elements would overlap
     if (it.prec32) {
-      float *sf = reinterpret_cast<float *>(smb) + 2 * tid;
+      const int st = slot4 ? T : 2 * T;
+      float *sf = reinterpret_cast<float *>(smb) + (slot4 ? tid : 2 * tid);
       if (it.dbl)
-        solve_row32<double>(it.gram, row, it.J, it.E, it.ldf, (double *)it.fac, lambda, cond_max, sf, 2 * T,
+        solve_row32<double>(it.gram, row, it.J, it.E, it.ldf, (double *)it.fac, lambda, cond_max, sf, st,
                             it.fp64_list, it.nfb + 1);
       else
-        solve_row32<float>(it.gram, row, it.J, it.E, it.ldf, (float *)it.fac, lambda, cond_max, sf, 2 * T,
+        solve_row32<float>(it.gram, row, it.J, it.E, it.ldf, (float *)it.fac, lambda, cond_max, sf, st,
                            it.fp64_list, it.nfb + 1);
     } else {
       double *A = reinterpret_cast<double *>(smb) + tid;
@@ -1839,14 +1842,21 @@ struct FusedBatch {
     uint32_t grid = 0;
     size_t args_off = 0, first_off = 0, img_off = 0;  // offsets into dev
   };
+  struct SolveGroup {  // the handles of one level with one rank and one solve path
+    size_t items_off = 0, first_off = 0;
+    int count = 0, threads = 0, slot4 = 0;
+    uint64_t rows = 0;
+    size_t smem = 0;
+  };
   struct Level {
     int count = 0;  // handles with a mode of this index
-    size_t zero_off = 0, zfirst_off = 0, solve_off = 0, sfirst_off = 0;
-    uint64_t zero_total = 0, rows_total = 0;
+    size_t zero_off = 0, zfirst_off = 0, solve_off = 0;
+    uint64_t zero_total = 0;
     bool any32 = false;
     int maxJ = 1;
-    size_t solve_smem = 0, list_smem = 0, lu_smem = 0;
+    size_t list_smem = 0, lu_smem = 0;
     std::vector<Group> groups;
+    std::vector<SolveGroup> solves;
   };
   std::vector<Level> levels;
   int count = 0;
@@ -1928,12 +1938,37 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
     }
     L.count = (int)si.size();
     L.zero_total = zf.back();
-    L.rows_total = sf.back();
     L.zero_off = put(zi.data(), zi.size() * sizeof(ZeroItem));
     L.zfirst_off = put(zf.data(), zf.size() * 8);
-    L.solve_off = put(si.data(), si.size() * sizeof(SolveItem));
-    L.sfirst_off = put(sf.data(), sf.size() * 8);
-    L.solve_smem = kSolveMultiThreads * std::max(max_e64, max_e32);
+    L.solve_off = put(si.data(), si.size() * sizeof(SolveItem));  // every handle: the list passes
+    // the row solves by (rank, path): each launch with the shared memory and block
+    // size the single-handle solve kernels use for that rank
+    {
+      std::vector<std::pair<int, int>> keys;
+      for (const SolveItem &x : si)
+        if (std::find(keys.begin(), keys.end(), std::make_pair(x.J, x.prec32)) == keys.end())
+          keys.emplace_back(x.J, x.prec32);
+      for (const auto &key : keys) {
+        std::vector<SolveItem> g;
+        std::vector<uint64_t> gf(1, 0);
+        for (size_t q = 0; q < si.size(); ++q)
+          if (si[q].J == key.first && si[q].prec32 == key.second) {
+            g.push_back(si[q]);
+            gf.push_back(gf.back() + (sf[q + 1] - sf[q]));
+          }
+        FusedBatch::SolveGroup G;
+        G.count = (int)g.size();
+        G.rows = gf.back();
+        G.threads = key.first <= 12 ? 128 : 64;
+        G.slot4 = key.second;
+        const size_t E = (size_t)pairs_for(key.first);
+        G.smem = (size_t)G.threads * (key.second ? (E + 3 * (size_t)key.first) * 4 : E * 8);
+        G.items_off = put(g.data(), g.size() * sizeof(SolveItem));
+        G.first_off = put(gf.data(), gf.size() * 8);
+        L.solves.push_back(G);
+      }
+    }
+    (void)max_e32;
     L.list_smem = kSolveMultiThreads * max_e64;
     L.lu_smem = (size_t)(kLuMultiThreads / 32) * ((size_t)L.maxJ * L.maxJ + L.maxJ) * 8;
     // kernel classes: the same multi-tensor kernel, shared memory and block
@@ -2003,7 +2038,7 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
   GTK_CUDA(cudaMemcpy(fb->dev, host.data(), host.size(), cudaMemcpyHostToDevice));
   size_t groups = 0;
   for (auto &L : fb->levels) groups = std::max(groups, L.groups.size());
-  const size_t nside = std::min<size_t>(groups, 4);
+  const size_t nside = std::min<size_t>(groups, 8);
   fb->side.assign(nside, nullptr);
   for (auto &s : fb->side) GTK_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
   size_t nev = 0;
@@ -2011,7 +2046,8 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
   fb->ev.assign(nev, nullptr);
   for (auto &e : fb->ev) GTK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (auto &L : fb->levels) {
-    if (int rc = prepare_fn((const void *)k_solve_multi, L.solve_smem)) return rc;
+    for (auto &G : L.solves)
+      if (int rc = prepare_fn((const void *)k_solve_multi, G.smem)) return rc;
     if (int rc = prepare_fn((const void *)k_solve_list64_multi, L.list_smem)) return rc;
     if (int rc = prepare_fn((const void *)k_solve_lu_multi, L.lu_smem)) return rc;
   }
@@ -2037,11 +2073,9 @@ int fused_batch_enqueue(FusedBatch *fb, cudaStream_t s, double *err_out, int *st
     GTK_CUDA(cudaEventRecord(fork, s));
     for (size_t gi = 0; gi < L.groups.size(); ++gi) {
       const FusedBatch::Group &g = L.groups[gi];
-      // classes that allocate tensor memory run one after another on the main
-      // stream (each kernel's residency limit keeps its CTAs within an SM's 512
-      // columns; two such kernels side by side could exceed it); the SIMT
-      // classes run beside them on side streams
-      cudaStream_t cs = (fb->side.empty() || g.proto.tmem) ? s : fb->side[gi % fb->side.size()];
+      // the classes run side by side on the side streams, as the tensors' own
+      // launch chains do in the per-handle graph
+      cudaStream_t cs = fb->side.empty() ? s : fb->side[gi % fb->side.size()];
       GTK_CUDA(cudaStreamWaitEvent(cs, fork, 0));
       const void *args = D + g.args_off;
       const void *first = D + g.first_off;
@@ -2062,12 +2096,15 @@ int fused_batch_enqueue(FusedBatch *fb, cudaStream_t s, double *err_out, int *st
       ++k;
     }
     const SolveItem *si = (const SolveItem *)(D + L.solve_off);
-    const uint64_t *sfirst = (const uint64_t *)(D + L.sfirst_off);
-    const unsigned sg = (unsigned)std::max<uint64_t>(
-        1, std::min<uint64_t>((L.rows_total + kSolveMultiThreads - 1) / kSolveMultiThreads, 65535));
-    k_solve_multi<<<sg, kSolveMultiThreads, L.solve_smem, s>>>(si, sfirst, n, kLambda, kCondMaxFp32);
-    GTK_CUDA(cudaGetLastError());
-    ++k;
+    for (const auto &G : L.solves) {
+      const unsigned sg =
+          (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((G.rows + G.threads - 1) / G.threads, 65535));
+      k_solve_multi<<<sg, G.threads, G.smem, s>>>((const SolveItem *)(D + G.items_off),
+                                                  (const uint64_t *)(D + G.first_off), G.count, kLambda, kCondMaxFp32,
+                                                  G.slot4);
+      GTK_CUDA(cudaGetLastError());
+      ++k;
+    }
     if (L.any32) {
       k_solve_list64_multi<<<(unsigned)(n * 2), kSolveMultiThreads, L.list_smem, s>>>(si, n, kLambda, 2);
       GTK_CUDA(cudaGetLastError());

@@ -254,8 +254,10 @@ def test_fused_batch_few_launches_match_one_by_one_and_oracle(monkeypatch):
             k_fused = b.kernels()
             maxN = max(len(c[0]) for c in FUSED)
             classes = len({(len(c[0]), c[2], c[5]) for c in FUSED})
-            # per mode index: zeroing + at most one launch per class + 3 solve passes; fit + reduction
-            assert 0 < k_fused <= maxN * (1 + classes + 3) + 2, k_fused
+            solve_groups = len({(c[2], c[5] != "plain") for c in FUSED})
+            # per mode index: zeroing + at most one launch per class + one row solve per (rank,
+            # path) + the FP64 and LU list passes; then fit + reduction
+            assert 0 < k_fused <= maxN * (1 + classes + solve_groups + 2) + 2, k_fused
             for i, c in enumerate(FUSED):
                 for n in range(len(c[0])):
                     assert rel_fro(batch_ts[i].get_factor(n), solo_ts[i].get_factor(n)) <= 1e-4, (i, n)
