@@ -1686,12 +1686,14 @@ __global__ void k_solve_multi(const SolveItem *__restrict__ items, const uint64_
   }
 }
 
-// the precision forms' FP64 list of every handle: `per` CTAs per handle
-__global__ void k_solve_list64_multi(const SolveItem *__restrict__ items, int count, double lambda, int per) {
+// the precision forms' FP64 list of every handle: handle i owns CTAs
+// [cta_first[i], cta_first[i + 1]) (its share grows with its row count)
+__global__ void k_solve_list64_multi(const SolveItem *__restrict__ items, const uint32_t *__restrict__ cta_first,
+                                     int count, double lambda) {
   extern __shared__ __align__(16) unsigned char smb[];
   const int T = blockDim.x, tid = threadIdx.x;
-  const int i = blockIdx.x / per, sub = blockIdx.x % per;
-  if (i >= count) return;
+  const int i = slot_of(cta_first, count, blockIdx.x);
+  const uint32_t sub = blockIdx.x - cta_first[i], per = cta_first[i + 1] - cta_first[i];
   const SolveItem &it = items[i];
   if (!it.prec32) return;
   const uint64_t n = it.nfb[1];
@@ -1706,12 +1708,13 @@ __global__ void k_solve_list64_multi(const SolveItem *__restrict__ items, int co
   }
 }
 
-// the pivoted-LU list of every handle, one warp per row, `per` CTAs per handle
-__global__ void k_solve_lu_multi(const SolveItem *__restrict__ items, int count, double lambda, int per, int maxJ) {
+// the pivoted-LU list of every handle, one warp per row, CTA ranges as above
+__global__ void k_solve_lu_multi(const SolveItem *__restrict__ items, const uint32_t *__restrict__ cta_first,
+                                 int count, double lambda, int maxJ) {
   extern __shared__ double sm[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  const int i = blockIdx.x / per, sub = blockIdx.x % per;
-  if (i >= count) return;
+  const int i = slot_of(cta_first, count, blockIdx.x);
+  const uint32_t sub = blockIdx.x - cta_first[i], per = cta_first[i + 1] - cta_first[i];
   const SolveItem &it = items[i];
   const int J = it.J;
   double *A = sm + (size_t)wib * ((size_t)maxJ * maxJ + maxJ);
@@ -1851,6 +1854,8 @@ struct FusedBatch {
   struct Level {
     int count = 0;  // handles with a mode of this index
     size_t zero_off = 0, zfirst_off = 0, solve_off = 0;
+    size_t list_first_off = 0, lu_first_off = 0;  // CTA ranges of the list passes
+    uint32_t list_grid = 0, lu_grid = 0;
     uint64_t zero_total = 0;
     bool any32 = false;
     int maxJ = 1;
@@ -1941,6 +1946,24 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
     L.zero_off = put(zi.data(), zi.size() * sizeof(ZeroItem));
     L.zfirst_off = put(zf.data(), zf.size() * 8);
     L.solve_off = put(si.data(), si.size() * sizeof(SolveItem));  // every handle: the list passes
+    {
+      // list passes: as many CTAs per handle as its rows could need, up to two per
+      // SM (the lists' lengths are known only on the device)
+      std::vector<uint32_t> lf(1, 0), uf(1, 0);
+      for (size_t q = 0; q < si.size(); ++q) {
+        const uint64_t rows = sf[q + 1] - sf[q];
+        const uint64_t cap = 2 * (uint64_t)ts[0]->num_sms;
+        lf.push_back(lf.back() + (uint32_t)std::max<uint64_t>(
+                                     1, std::min<uint64_t>((rows + kSolveMultiThreads - 1) / kSolveMultiThreads, cap)));
+        uf.push_back(uf.back() + (uint32_t)std::max<uint64_t>(
+                                     1, std::min<uint64_t>((rows + kLuMultiThreads / 32 - 1) / (kLuMultiThreads / 32),
+                                                           cap)));
+      }
+      L.list_grid = lf.back();
+      L.lu_grid = uf.back();
+      L.list_first_off = put(lf.data(), lf.size() * 4);
+      L.lu_first_off = put(uf.data(), uf.size() * 4);
+    }
     // the row solves by (rank, path): each launch with the shared memory and block
     // size the single-handle solve kernels use for that rank
     {
@@ -2106,11 +2129,13 @@ int fused_batch_enqueue(FusedBatch *fb, cudaStream_t s, double *err_out, int *st
       ++k;
     }
     if (L.any32) {
-      k_solve_list64_multi<<<(unsigned)(n * 2), kSolveMultiThreads, L.list_smem, s>>>(si, n, kLambda, 2);
+      k_solve_list64_multi<<<L.list_grid, kSolveMultiThreads, L.list_smem, s>>>(
+          si, (const uint32_t *)(D + L.list_first_off), n, kLambda);
       GTK_CUDA(cudaGetLastError());
       ++k;
     }
-    k_solve_lu_multi<<<(unsigned)(n * 2), kLuMultiThreads, L.lu_smem, s>>>(si, n, kLambda, 2, L.maxJ);
+    k_solve_lu_multi<<<L.lu_grid, kLuMultiThreads, L.lu_smem, s>>>(si, (const uint32_t *)(D + L.lu_first_off), n,
+                                                                   kLambda, L.maxJ);
     GTK_CUDA(cudaGetLastError());
     ++k;
   }
