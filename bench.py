@@ -101,8 +101,9 @@ def args_parse():
                         "rank-16 tensor in plain FP32, BF16 and TF32 against an FP64 run")
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--batch-max-nnz", type=int, default=5_000_000, help="upper end of the per-tensor nnz range")
-    p.add_argument("--ws-train-seeds", type=int, default=24, help="training tensors of the warm-start family")
-    p.add_argument("--ws-held-seeds", type=int, default=6, help="held-out tensors of the warm-start family")
+    p.add_argument("--ws-train-seeds", type=int, default=200,
+                   help="training tensors of the warm-start family (the configuration's 200; ~40 min in all)")
+    p.add_argument("--ws-held-seeds", type=int, default=50, help="held-out tensors of the warm-start family")
     p.add_argument("--ws-nnz", type=int, default=20_000_000, help="observed entries per warm-start tensor")
     return p.parse_args()
 

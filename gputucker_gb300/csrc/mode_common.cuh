@@ -40,6 +40,60 @@ struct ModeArgs {
   const void *core;                  // the core, linear order (last mode fastest): ref_order
 };
 
+// A multi-tensor launch (batches): up to kMultiMax handles of one kernel class,
+// handle i owning CTAs [first[i], first[i + 1]).  Passed by value as a
+// __grid_constant__ kernel parameter (under the 32 KB parameter limit), so the
+// kernels read the argument blocks from the constant bank as a single-handle
+// launch reads its ModeArgs.
+constexpr int kMultiMax = 96;
+struct MultiParams {
+  ModeArgs args[kMultiMax];
+  const unsigned char *img[kMultiMax];  // streamed-core class: each handle's core image
+  uint32_t first[kMultiMax + 1];
+  int count;
+};
+static_assert(sizeof(MultiParams) <= 32000, "kernel parameter limit");
+
+// This CTA's handle of a multi-tensor launch: its argument block copied into
+// shared memory (the kernels then read fields as a single-handle launch reads
+// its parameters, reloading them after barriers instead of holding them in
+// registers); returns the CTA's index and count within the handle's range.
+__device__ __forceinline__ const ModeArgs &multi_select(const MultiParams &p, ModeArgs &sa, uint32_t &cta,
+                                                        uint32_t &nctas, const unsigned char **img = nullptr) {
+  int lo = 0, hi = p.count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (p.first[mid] <= blockIdx.x)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int i = lo;
+  constexpr int W = (int)(sizeof(ModeArgs) / 8);
+  static_assert(sizeof(ModeArgs) % 8 == 0, "argument block in 8-byte words");
+  const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&p.args[i]);
+  unsigned long long *dst = reinterpret_cast<unsigned long long *>(&sa);
+  for (int k = threadIdx.x; k < W; k += blockDim.x) dst[k] = src[k];
+  __syncthreads();
+  cta = blockIdx.x - p.first[i];
+  nctas = p.first[i + 1] - p.first[i];
+  if (img) *img = p.img[i];
+  return sa;
+}
+
+// the entry i with first[i] <= b < first[i + 1] of a parameter-space table
+__device__ __forceinline__ int slot_of_param(const uint32_t *first, int count, uint32_t b) {
+  int lo = 0, hi = count - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (first[mid] <= b)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 // the entry i of a multi-tensor launch whose CTA range [first[i], first[i + 1])
 // holds CTA b (first[0] = 0, first[count] = the grid)
 __device__ __forceinline__ int slot_of(const uint32_t *__restrict__ first, int count, uint32_t b) {

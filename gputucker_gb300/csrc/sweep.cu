@@ -287,10 +287,11 @@ __global__ void __launch_bounds__(kThreads) k_mode_spec(ModeArgs a) {
 // Many tensors of one shape class in one launch (batches): CTA b works for
 // tensor i with cta_first[i] <= b < cta_first[i + 1], on that tensor's tiles
 template <class V, int N, int J, int NPT, int KIND, bool STREAM = false>
-__global__ void __launch_bounds__(kThreads)
-    k_mode_spec_multi(const ModeArgs *__restrict__ args, const uint32_t *__restrict__ cta_first, int count) {
-  const int i = slot_of(cta_first, count, blockIdx.x);
-  mode_spec_body<V, N, J, NPT, KIND, STREAM>(args[i], blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
+__global__ void __launch_bounds__(kThreads) k_mode_spec_multi(const __grid_constant__ MultiParams p) {
+  __shared__ ModeArgs sa;
+  uint32_t cta, nctas;
+  const ModeArgs &a = multi_select(p, sa, cta, nctas);
+  mode_spec_body<V, N, J, NPT, KIND, STREAM>(a, cta, nctas);
 }
 
 // ---------------------------------------------------------------- generic kernel
@@ -1842,8 +1843,7 @@ struct FusedBatch {
   struct Group {  // one kernel class of one level
     MultiDesc proto;
     int count = 0;
-    uint32_t grid = 0;
-    size_t args_off = 0, first_off = 0, img_off = 0;  // offsets into dev
+    std::vector<std::unique_ptr<MultiParams>> chunks;  // launches of up to kMultiMax handles
   };
   struct SolveGroup {  // the handles of one level with one rank and one solve path
     size_t items_off = 0, first_off = 0;
@@ -2008,20 +2008,19 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
       g->count += 1;
     }
     for (auto &g : L.groups) {
-      std::vector<unsigned char> args;
-      std::vector<uint32_t> first(1, 0);
-      std::vector<const unsigned char *> imgs;
       for (auto &pd : descs) {
         const MultiDesc &d = pd.first;
         if (d.fn != g.proto.fn || d.smem != g.proto.smem || d.threads != g.proto.threads) continue;
-        args.insert(args.end(), d.args, d.args + sizeof(ModeArgs));  // the kernels index a ModeArgs array
-        first.push_back(first.back() + d.ctas);
-        imgs.push_back(d.image);
+        if (g.chunks.empty() || g.chunks.back()->count == kMultiMax) {
+          g.chunks.emplace_back(new MultiParams());
+          memset(g.chunks.back().get(), 0, sizeof(MultiParams));
+        }
+        MultiParams &mp = *g.chunks.back();
+        memcpy(&mp.args[mp.count], d.args, sizeof(ModeArgs));
+        mp.img[mp.count] = d.image;
+        mp.first[mp.count + 1] = mp.first[mp.count] + d.ctas;
+        mp.count += 1;
       }
-      g.grid = first.back();
-      g.args_off = put(args.data(), args.size());
-      g.first_off = put(first.data(), first.size() * 4);
-      g.img_off = put(imgs.data(), imgs.size() * sizeof(void *));
     }
     fb->levels.push_back(std::move(L));
   }
@@ -2100,23 +2099,16 @@ int fused_batch_enqueue(FusedBatch *fb, cudaStream_t s, double *err_out, int *st
       // launch chains do in the per-handle graph
       cudaStream_t cs = fb->side.empty() ? s : fb->side[gi % fb->side.size()];
       GTK_CUDA(cudaStreamWaitEvent(cs, fork, 0));
-      const void *args = D + g.args_off;
-      const void *first = D + g.first_off;
-      const void *imgs = D + g.img_off;
-      int cnt = g.count;
-      if (g.proto.with_image) {
-        void *p[] = {&args, &imgs, &first, &cnt};
-        GTK_CUDA(cudaLaunchKernel(g.proto.fn, dim3(g.grid), dim3(g.proto.threads), p, g.proto.smem, cs));
-      } else {
-        void *p[] = {&args, &first, &cnt};
-        GTK_CUDA(cudaLaunchKernel(g.proto.fn, dim3(g.grid), dim3(g.proto.threads), p, g.proto.smem, cs));
+      for (const auto &mp : g.chunks) {
+        void *p[] = {mp.get()};
+        GTK_CUDA(cudaLaunchKernel(g.proto.fn, dim3(mp->first[mp->count]), dim3(g.proto.threads), p, g.proto.smem, cs));
       }
       cudaEvent_t join = fb->ev[ev++];
       if (cs != s) {
         GTK_CUDA(cudaEventRecord(join, cs));
         GTK_CUDA(cudaStreamWaitEvent(s, join, 0));
       }
-      ++k;
+      k += g.chunks.size();
     }
     const SolveItem *si = (const SolveItem *)(D + L.solve_off);
     for (const auto &G : L.solves) {

@@ -365,14 +365,14 @@ __global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs(ModeArgs a, const un
   mode_tcs_body<N, J, KIND>(a, bimg, blockIdx.x, gridDim.x);
 }
 
-// many tensors of one shape class in one launch (batches), as k_mode_spec_multi;
-// bimgs[i]: tensor i's core image of the mode
+// many tensors of one shape class in one launch (batches), as k_mode_spec_multi
 template <int N, int J, int KIND>
-__global__ void __launch_bounds__(kTsThreads, 1)
-    k_mode_tcs_multi(const ModeArgs *__restrict__ args, const unsigned char *const *__restrict__ bimgs,
-                     const uint32_t *__restrict__ cta_first, int count) {
-  const int i = slot_of(cta_first, count, blockIdx.x);
-  mode_tcs_body<N, J, KIND>(args[i], bimgs[i], blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
+__global__ void __launch_bounds__(kTsThreads, 1) k_mode_tcs_multi(const __grid_constant__ MultiParams p) {
+  __shared__ ModeArgs sa;
+  uint32_t cta, nctas;
+  const unsigned char *img = nullptr;
+  const ModeArgs &a = multi_select(p, sa, cta, nctas, &img);
+  mode_tcs_body<N, J, KIND>(a, img, cta, nctas);
 }
 
 struct TsLaunch {

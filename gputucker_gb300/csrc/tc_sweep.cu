@@ -355,10 +355,11 @@ __global__ void __launch_bounds__(kTcThreads) k_mode_tc(ModeArgs a) {
 
 // many tensors of one shape class in one launch (batches), as k_mode_spec_multi
 template <int J, int D, int PREC, int KIND>
-__global__ void __launch_bounds__(kTcThreads)
-    k_mode_tc_multi(const ModeArgs *__restrict__ args, const uint32_t *__restrict__ cta_first, int count) {
-  const int i = slot_of(cta_first, count, blockIdx.x);
-  mode_tc_body<J, D, PREC, KIND>(args[i], blockIdx.x - cta_first[i], cta_first[i + 1] - cta_first[i]);
+__global__ void __launch_bounds__(kTcThreads) k_mode_tc_multi(const __grid_constant__ MultiParams p) {
+  __shared__ ModeArgs sa;
+  uint32_t cta, nctas;
+  const ModeArgs &a = multi_select(p, sa, cta, nctas);
+  mode_tc_body<J, D, PREC, KIND>(a, cta, nctas);
 }
 
 struct TcLaunch {
