@@ -12,7 +12,10 @@
 // chains are independent branches of the graph, so the GPU runs them
 // concurrently -- small tensors, which alone cannot fill 152 SMs, fill it
 // together -- and a sweep of the whole batch costs one graph launch and one
-// device-to-host copy.  Each tensor keeps its own kernels (chosen by order, rank
+// device-to-host copy.  GTK_BATCH_FUSED=1 puts the fused sweep in the graph
+// instead (sweep.cu, FusedBatch: per mode index one launch per kernel class for
+// every handle of the class, batched row solves, one fit): 30x fewer launches,
+// measured 8-30 % slower, since it waits for every handle at each mode.  Each tensor keeps its own kernels (chosen by order, rank
 // and precision, or by the autotuner), its own buffers and its own results;
 // factor and core contents may change between sweeps.  A change of a tensor's
 // precision or kernel variant is seen at the next sweep, which captures anew.
@@ -328,9 +331,11 @@ int gtk_batch_sweep(gtk_batch *b, double *fits) {
       for (gtk_tensor *t : b->ts)
         if (sweep_needs_dstore(*t))
           if (int rc = ensure_dstore(*t)) return rc;
-      // the few-launch form where every handle has one (GTK_BATCH_FUSED=0: per-handle launches)
+      // GTK_BATCH_FUSED=1: the few-launch form where every handle has one; by
+      // default one launch chain per handle (measured faster: the handles' chains
+      // overlap freely, while the fused form waits for every handle at each mode)
       const char *fz = getenv("GTK_BATCH_FUSED");
-      if (!b->fused && !(fz && *fz == '0')) {
+      if (!b->fused && fz && *fz == '1') {
         std::vector<DevTensor *> ts(b->ts.begin(), b->ts.end());
         const int rc = fused_batch_build(ts, &b->fused);
         if (rc && rc != GTK_ERR_UNSUPPORTED) return rc;

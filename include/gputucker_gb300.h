@@ -285,7 +285,12 @@ int gtk_autotune(gtk_tensor *t, int *variant);
  * their own between batch sweeps (not concurrently with one); a change of a
  * handle's precision or variant recaptures the graph.  Destroy the batch before
  * its handles.  gtk_batch_kernels: kernels in one replay of the graph (0 before
- * the first capture). */
+ * the first capture).  With GTK_BATCH_FUSED=1 in the environment when the batch
+ * first sweeps, the graph holds the fused sweep instead: per mode index one
+ * kernel zeroing every handle's Gram/RHS, one update launch per kernel class
+ * for every handle of that class, the row solves batched per (rank, path), one
+ * fit launch and one reduction (FP32 handles of rank <= 24 without the
+ * reference-order variant; others fall back to per-handle launches). */
 typedef struct gtk_batch gtk_batch;
 int gtk_batch_create(gtk_tensor *const *tensors, int count, gtk_batch **out);
 int gtk_batch_sweep(gtk_batch *b, double *fits);

@@ -237,11 +237,12 @@ FUSED = [
 
 
 def test_fused_batch_few_launches_match_one_by_one_and_oracle(monkeypatch):
-    """The fused sweep (per mode index: one zeroing kernel, one launch per update
-    kernel class, the batched row solves; one fit and one reduction) against the
-    same handles swept one by one, against the per-handle graph
-    (GTK_BATCH_FUSED=0), and three members against the FP64 oracle."""
+    """The fused sweep (GTK_BATCH_FUSED=1; per mode index: one zeroing kernel, one
+    launch per update kernel class, the batched row solves; one fit and one
+    reduction) against the same handles swept one by one, against the default
+    per-handle graph, and three members against the FP64 oracle."""
     from oracle_util import Oracle
+    monkeypatch.setenv("GTK_BATCH_FUSED", "1")
     pairs = [_make(c, 200 + i) for i, c in enumerate(FUSED)]
     batch_ts = [p[0] for p in pairs]
     solo_ts = [p[1] for p in pairs]
@@ -271,7 +272,7 @@ def test_fused_batch_few_launches_match_one_by_one_and_oracle(monkeypatch):
             assert b2.kernels() > k_fused
         for t in batch_ts:
             t.init_random(1, 0)
-        monkeypatch.delenv("GTK_BATCH_FUSED")
+        monkeypatch.setenv("GTK_BATCH_FUSED", "1")
         with gtk.Batch(batch_ts) as b3:
             f3 = [b3.sweep() for _ in range(2)][-1]
         assert np.all(np.abs(f3 - f2) <= 1e-6), (f3, f2)
