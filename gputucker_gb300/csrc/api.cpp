@@ -532,6 +532,7 @@ int gtk_create_blocks(const gtk_coo *coo, const uint32_t *P, int rank, int devic
       for (int k = 0; k < N; ++k) A((void **)&t->vidx[n][k], nnz * 4);
     }
     A(&t->fac[n], t->rows[n] * t->ldf * vs);
+    if (vs == 4 && t->ldf == 12) A(&t->gfac[n], t->rows[n] * 64);
     A(&t->corep[n], (core_n / rank) * t->ldf * vs);
   }
   A(&t->core, core_n * vs);
@@ -809,7 +810,10 @@ int gtk_tucker_decomposition(gtk_tensor *t, int max_iters, double tol, double *f
   int numeric = 0;
   while (true) {
     if (int rc = run_sweep(*t, &fit)) return rc;
-    if (check_status(*t)) numeric = GTK_ERR_NUMERIC;
+    if (int rc = check_status(*t)) {  // a singular row is reported at the end; anything else ends the run
+      if (rc != GTK_ERR_NUMERIC) return rc;
+      numeric = rc;
+    }
     if (fits) fits[it] = fit;
     ++it;
     if (it >= max_iters || (p_fit != -1 && std::fabs(p_fit - fit) <= tol)) break;

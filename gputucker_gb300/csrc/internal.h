@@ -181,6 +181,9 @@ struct DevTensor {
   void *vval[kMaxOrder] = {};
   uint32_t *vperm[kMaxOrder] = {};  // view position -> block-major position
   void *fac[kMaxOrder] = {};
+  // f32 handles with ldf = 12 (J = 9..12): the factors again with 64-byte rows,
+  // which the tensor-core kernels gather from (refreshed before each launch)
+  void *gfac[kMaxOrder] = {};
   void *core = nullptr;
   void *corep[kMaxOrder] = {};
   double *gram = nullptr;
@@ -277,6 +280,18 @@ struct DevBuf {
 
 // ---- batches: kernels shared by many handles per launch (gtk_batch_sweep)
 constexpr size_t kModeArgsBytes = 320;
+// Gather copies of FP32 factor rows of 12 floats (48 bytes, every other one off
+// a 32-byte boundary) as 64-byte rows, which the tensor-core kernels read with
+// one 256-bit load and one 64- or 128-bit load: two sector accesses per row
+// instead of three 16-byte loads' three.
+struct PadItem {
+  const float *src;  // [rows][12]
+  float *dst;        // [rows][16]
+};
+// the copies the tensor-core kernels of `mode` read (none unless ldf = 12),
+// appended with the prefix of their row counts (tc_sweep.cu)
+int tc_gather_items(const DevTensor &t, int mode, std::vector<PadItem> *items, std::vector<uint64_t> *first);
+
 // One handle's mode update in the form its kernel class's multi-tensor kernel takes
 struct MultiDesc {
   const void *fn = nullptr;              // k_mode_*_multi<...> of the class

@@ -23,7 +23,10 @@ template <int B> struct Pow<B, 0> { static constexpr int v = 1; };
 struct ModeArgs {
   const uint32_t *coord[kMaxOrder];  // view coordinates (global), coord[mode] = row
   const void *val;                   // view values
-  const void *fac[kMaxOrder];        // factor matrices, row stride ldf
+  // factor matrices, row stride ldf; in the tensor-core kernels' arguments the
+  // other modes' entries of an ldf = 12 handle point at its gather copies
+  // (DevTensor::gfac, 64-byte rows)
+  const void *fac[kMaxOrder];
   const void *corep;                 // [J^(N-1)][ldf], mode first
   const uint32_t *vperm;             // view -> block-major position (kDelta)
   void *out;                         // kDelta: delta [nnz][J] block-major
@@ -39,6 +42,14 @@ struct ModeArgs {
   int ref_order;                     // generic kernel: delta in the reference's operation order
   const void *core;                  // the core, linear order (last mode fastest): ref_order
 };
+
+// row r of a gather copy (PadItem); floats 12..15 of a copied row are never read
+__device__ __forceinline__ void pad_row(const PadItem &it, uint64_t r) {
+  const float4 *s = reinterpret_cast<const float4 *>(it.src + r * 12);
+  float4 *d = reinterpret_cast<float4 *>(it.dst + r * 16);
+  const float4 a = __ldg(s), b = __ldg(s + 1), c = __ldg(s + 2);
+  d[0] = a, d[1] = b, d[2] = c;
+}
 
 // A multi-tensor launch (batches): up to kMultiMax handles of one kernel class,
 // handle i owning CTAs [first[i], first[i + 1]).  Passed by value as a
@@ -505,9 +516,10 @@ template <int J> struct GramBlk {
   }
 };
 
-// GramMma's delta-row stride: 8 or 24 floats, so that the fragment loads of a warp
-// (rows c, c + 4 of 8, columns g, g + 8, g + 16) hit 32 distinct banks
-__host__ __device__ constexpr int gram_mma_ldd(int J) { return J + 1 <= 8 ? 8 : 24; }
+// GramMma's delta-row stride: 8, 24 or 40 floats (8 or 24 mod 32), so that the
+// fragment loads of a warp (rows c, c + 4 of 8, columns g, g + 8, g + 16) hit 32
+// distinct banks; GramMma::off gives the row offsets
+__host__ __device__ constexpr int gram_mma_ldd(int J) { return J + 1 <= 8 ? 8 : J + 1 <= 16 ? 24 : 40; }
 
 // One warp's Gram/RHS reduction of its 32 delta rows on the tensor cores, for
 // J <= 16 (features f = [delta, x]).  For a run [a, b) of nonzeros of one row,
@@ -529,7 +541,7 @@ template <int J> struct GramMma {
   static constexpr int NT = (F + 7) / 8;  // 8-column n-tiles
   static constexpr int LDD = gram_mma_ldd(J);
   static constexpr int COLS = 8 * NT;  // columns a row must hold (features, then zeros)
-  static_assert(COLS <= LDD, "row stride");
+  static_assert(COLS + (LDD > 8 ? 4 : 0) <= LDD, "row stride");
   ProdSum<float> acc[NT][4];
   uint32_t row = 0xFFFFFFFFu;
 
@@ -547,13 +559,25 @@ template <int J> struct GramMma {
         : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
         : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
   }
-  // this lane's row of the delta tile: delta, x, zeros up to COLS (16-byte stores)
-  __device__ static void store_row(float *dx_row, const float (&delta)[J], float x) {
+  // Delta-tile layout: feature c of row r at r * LDD + c + pad(r), pad(r) = 4 for
+  // rows with bit 2 set (LDD 24, 40; 0 at LDD 8, whose rows have no room).  A row
+  // store (lane r writes its row as 16-byte chunks) then puts the 8 lanes of a
+  // quarter-warp on 8 distinct 4-bank groups: (LDD r + pad(r)) mod 32 over
+  // r = 0..7 is {0, 24, 16, 8, 4, 28, 20, 12} at LDD 24 and {0, 8, .., 24, 4, .., 28}
+  // at LDD 40, where the plain stride repeats after 4 rows (a 2-way conflict).
+  // The fragment loads stay conflict-free: rows k0 + c (k0 % 8 = 0, c < 4) have
+  // no pad and rows k0 + c + 4 all have the same one.
+  static constexpr int PAD = LDD > 8 ? 4 : 0;
+  __host__ __device__ static constexpr int pad(int r) { return PAD * ((r >> 2) & 1); }
+  __host__ __device__ static constexpr int off(int r, int c) { return r * LDD + c + pad(r); }
+  // row r of the warp's delta tile dx: delta, x, zeros up to COLS (16-byte stores)
+  __device__ static void store_row(float *dx, int r, const float (&delta)[J], float x) {
     float v[COLS];
 #pragma unroll
     for (int k = 0; k < COLS; ++k) v[k] = k < J ? delta[k] : k == J ? x : 0.f;
+    float *row = dx + off(r, 0);
 #pragma unroll
-    for (int k = 0; k < COLS; k += 4) *reinterpret_cast<float4 *>(dx_row + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+    for (int k = 0; k < COLS; k += 4) *reinterpret_cast<float4 *>(row + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
   }
   __device__ void flush(double *gram, int E, int lane) {
     if (row != 0xFFFFFFFFu) {
@@ -574,7 +598,7 @@ template <int J> struct GramMma {
   // rows k0 .. k0 + 7 of the delta tile, restricted (MASK) to the run [a, b)
   template <bool MASK>
   __device__ static void kstep(float (&d)[NT][4], const float *dx, int k0, int a, int b, int g, int c) {
-    const float *r0 = dx + (k0 + c) * LDD + g, *r1 = dx + (k0 + c + 4) * LDD + g;
+    const float *r0 = dx + (k0 + c) * LDD + g, *r1 = dx + (k0 + c + 4) * LDD + PAD + g;
     uint32_t h0, l0, h2, l2, h1 = 0, l1 = 0, h3 = 0, l3 = 0, h4 = 0, l4 = 0, h5 = 0, l5 = 0;
     split(r0[0], h0, l0);
     split(r1[0], h2, l2);

@@ -1630,14 +1630,23 @@ struct ZeroItem {
   unsigned int *nfb;
 };
 // every handle's Gram/RHS rows of the level's mode (first: prefix of the doubles),
-// and its per-mode LU / FP64 list counts
-__global__ void k_batch_zero(const ZeroItem *__restrict__ items, const uint64_t *__restrict__ first, int count) {
+// its per-mode LU / FP64 list counts, and the gather copies its tensor-core
+// kernel reads (pfirst: prefix of their rows)
+__global__ void k_batch_zero(const ZeroItem *__restrict__ items, const uint64_t *__restrict__ first, int count,
+                             const PadItem *__restrict__ pads, const uint64_t *__restrict__ pfirst, int npads) {
   const uint64_t total = first[count];
-  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (uint64_t)gridDim.x * blockDim.x;
   if (g < (uint64_t)count) items[g].nfb[0] = items[g].nfb[1] = 0u;
-  for (uint64_t k = g; k < total; k += (uint64_t)gridDim.x * blockDim.x) {
+  for (uint64_t k = g; k < total; k += stride) {
     const int i = slot_of64(first, count, k);
     items[i].gram[k - first[i]] = 0.0;
+  }
+  if (npads) {
+    const uint64_t ptotal = pfirst[npads];
+    for (uint64_t k = g; k < ptotal; k += stride) {
+      const int i = slot_of64(pfirst, npads, k);
+      pad_row(pads[i], k - pfirst[i]);
+    }
   }
 }
 
@@ -1854,6 +1863,9 @@ struct FusedBatch {
   struct Level {
     int count = 0;  // handles with a mode of this index
     size_t zero_off = 0, zfirst_off = 0, solve_off = 0;
+    size_t pad_off = 0, pfirst_off = 0;  // the gather copies to refresh (tensor-core handles with ldf 12)
+    int npads = 0;
+    uint64_t pad_total = 0;
     size_t list_first_off = 0, lu_first_off = 0;  // CTA ranges of the list passes
     uint32_t list_grid = 0, lu_grid = 0;
     uint64_t zero_total = 0;
@@ -1911,6 +1923,8 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
     std::vector<uint64_t> zf(1, 0);
     std::vector<SolveItem> si;
     std::vector<uint64_t> sf(1, 0);
+    std::vector<PadItem> pi;
+    std::vector<uint64_t> pf(1, 0);
     size_t max_e64 = 0, max_e32 = 0;
     std::vector<std::pair<MultiDesc, DevTensor *>> descs;
     for (DevTensor *t : ts) {
@@ -1918,6 +1932,7 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
       MultiDesc d;
       int rc = tc_update(*t) ? tc_multi_desc(*t, n, &d) : spec_multi_desc<float>(*t, n, &d);
       if (rc) return rc;
+      if (tc_update(*t) && (rc = tc_gather_items(*t, n, &pi, &pf))) return rc;
       descs.emplace_back(d, t);
       const int E = pairs_for(t->J);
       zi.push_back({t->gram, t->nfallback});
@@ -1945,6 +1960,12 @@ int fused_batch_build(const std::vector<DevTensor *> &ts, FusedBatch **out) {
     L.zero_total = zf.back();
     L.zero_off = put(zi.data(), zi.size() * sizeof(ZeroItem));
     L.zfirst_off = put(zf.data(), zf.size() * 8);
+    L.npads = (int)pi.size();
+    L.pad_total = pf.back();
+    if (L.npads) {
+      L.pad_off = put(pi.data(), pi.size() * sizeof(PadItem));
+      L.pfirst_off = put(pf.data(), pf.size() * 8);
+    }
     L.solve_off = put(si.data(), si.size() * sizeof(SolveItem));  // every handle: the list passes
     {
       // list passes: as many CTAs per handle as its rows could need, up to two per
@@ -2084,9 +2105,12 @@ int fused_batch_enqueue(FusedBatch *fb, cudaStream_t s, double *err_out, int *st
   for (auto &L : fb->levels) {
     const int n = L.count;
     {
-      const uint64_t blocks = std::max<uint64_t>((L.zero_total + 255) / 256, (uint64_t)(n + 255) / 256);
+      const uint64_t blocks = std::max<uint64_t>(std::max<uint64_t>((L.zero_total + 255) / 256, (L.pad_total + 255) / 256),
+                                                 (uint64_t)(n + 255) / 256);
       k_batch_zero<<<(unsigned)std::min<uint64_t>(blocks, 8192), 256, 0, s>>>(
-          (const ZeroItem *)(D + L.zero_off), (const uint64_t *)(D + L.zfirst_off), n);
+          (const ZeroItem *)(D + L.zero_off), (const uint64_t *)(D + L.zfirst_off), n,
+          L.npads ? (const PadItem *)(D + L.pad_off) : nullptr, L.npads ? (const uint64_t *)(D + L.pfirst_off) : nullptr,
+          L.npads);
       GTK_CUDA(cudaGetLastError());
       ++k;
     }

@@ -60,7 +60,7 @@ template <int J, int D, int PREC> struct TcShape {
   // Gram/RHS reduction: on the tensor cores (GramMma) for J <= 16, else GramBlk
   static constexpr bool GRAM_MMA = J <= 16;
   using Gram = std::conditional_t<GRAM_MMA, GramMma<J>, GramBlk<J>>;
-  // delta-tile row stride: GramMma's bank-conflict-free stride, or even for
+  // delta-tile row stride: GramMma's (rows padded by bit 2, GramMma::off), or even for
   // GramBlk's 64-bit pair loads (column J + 1 zero)
   static constexpr int LDD = GRAM_MMA ? gram_mma_ldd(J) : (J + 2) / 2 * 2;
   static constexpr int E = (J + 1) * (J + 2) / 2 - 1;
@@ -71,13 +71,68 @@ template <int J, int D, int PREC> struct TcShape {
   // reduction has read them
   static constexpr int OFF_DX = 0;
   static constexpr int WARP_A_BYTES = 32 * KP * ES;
-  static_assert(32 * LDD * 4 <= WARP_A_BYTES, "a warp's delta rows must fit in its A rows");
+  static_assert(32 * LDD * 4 <= WARP_A_BYTES, "a warp's delta rows must fit in its A rows");  // pads included
   static constexpr int OFF_ROWS = (OFF_B + B_BYTES + 15) / 16 * 16;
   static constexpr int OFF_BAR = OFF_ROWS + (kTcThreads * 4 + 15) / 16 * 16;
   static constexpr int OFF_SLOT = OFF_BAR + 16;
   static constexpr int SMEM = OFF_SLOT + 16;
 };
 
+
+// element (r, c) of a warp's delta tile
+template <class S> __device__ __forceinline__ int tile_off(int r, int c) {
+  if constexpr (S::GRAM_MMA)
+    return S::Gram::off(r, c);
+  else
+    return r * S::LDD + c;
+}
+
+// Row r of a factor matrix with LDG floats per row (LDG in {4, 8, 12, 16}), rank
+// J.  A warp's gather costs the L1 one wavefront per sector each lane touches, and
+// the L1 is the busiest unit of this kernel, so rows are read with as few sector
+// accesses as they span: 256-bit loads of 32-byte-aligned rows (LDG 8, 16: the
+// factors themselves; LDG 12: the gather copy with 64-byte rows, a 256-bit load
+// and a 64-bit (J <= 10) or 128-bit one).  Factor matrices and gather copies start
+// on 32-byte boundaries, which run_mode_tc checks.
+template <int J, int LDG> struct FRow {
+  static_assert(LDG == 4 || LDG == 8 || LDG == 12 || LDG == 16, "factor row stride");
+  static constexpr int STRIDE = LDG == 12 ? 16 : LDG;  // floats between the rows read
+  float v[LDG];
+  __device__ __forceinline__ void load(const float *base, uint32_t r) {
+    const float *row = base + (size_t)r * STRIDE;
+    if constexpr (LDG == 4) {
+      const float4 u = __ldg(reinterpret_cast<const float4 *>(row));
+      v[0] = u.x, v[1] = u.y, v[2] = u.z, v[3] = u.w;
+    } else if constexpr (LDG == 12) {
+      ldg256(row, v);
+      if constexpr (J <= 10) {
+        const float2 u = __ldg(reinterpret_cast<const float2 *>(row + 8));
+        v[8] = u.x, v[9] = u.y, v[10] = v[11] = 0.f;  // entries J.. are never read
+      } else {
+        const float4 u = __ldg(reinterpret_cast<const float4 *>(row + 8));
+        v[8] = u.x, v[9] = u.y, v[10] = u.z, v[11] = u.w;
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < LDG / 8; ++c) ldg256(row + 8 * c, v + 8 * c);
+    }
+  }
+};
+
+// a handle's gather copies (the listed factors; first: prefix of their rows)
+struct PadList {
+  PadItem it[kMaxOrder];
+  uint64_t first[kMaxOrder + 1];
+  int n;
+};
+__global__ void k_pad_rows(const __grid_constant__ PadList L) {
+  const uint64_t total = L.first[L.n];
+  for (uint64_t k = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (uint64_t)gridDim.x * blockDim.x) {
+    int i = 0;
+    while (k >= L.first[i + 1]) ++i;
+    pad_row(L.it[i], k - L.first[i]);
+  }
+}
 
 template <int J, int D, int PREC, int KIND>
 __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, uint32_t nctas) {
@@ -145,7 +200,7 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
   struct TileIn {
     uint32_t row;
     float x;
-    float p[LDG], q[LDG], e1[LDG];
+    FRow<J, LDG> p, q, e1;
   };
   auto load_crd = [&](uint64_t tl, TileCrd &c) {
     const uint64_t b0 = tl * kTcThreads;
@@ -161,25 +216,9 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
   auto load_rows = [&](const TileCrd &c, TileIn &in) {
     in.row = c.row;
     in.x = c.x;
-    const float4 *fp = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 2]]) +
-                                                        (size_t)c.ip * LDG);
-    const float4 *fq = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[D - 1]]) +
-                                                        (size_t)c.iq * LDG);
-#pragma unroll
-    for (int k = 0; k < LDG / 4; ++k) {
-      const float4 u = __ldg(fp + k), w = __ldg(fq + k);
-      in.p[4 * k] = u.x, in.p[4 * k + 1] = u.y, in.p[4 * k + 2] = u.z, in.p[4 * k + 3] = u.w;
-      in.q[4 * k] = w.x, in.q[4 * k + 1] = w.y, in.q[4 * k + 2] = w.z, in.q[4 * k + 3] = w.w;
-    }
-    if (D == 3) {
-      const float4 *fe = reinterpret_cast<const float4 *>(reinterpret_cast<const float *>(a.fac[a.others[0]]) +
-                                                          (size_t)c.ie * LDG);
-#pragma unroll
-      for (int k = 0; k < LDG / 4; ++k) {
-        const float4 u = __ldg(fe + k);
-        in.e1[4 * k] = u.x, in.e1[4 * k + 1] = u.y, in.e1[4 * k + 2] = u.z, in.e1[4 * k + 3] = u.w;
-      }
-    }
+    in.p.load(reinterpret_cast<const float *>(a.fac[a.others[D - 2]]), c.ip);
+    in.q.load(reinterpret_cast<const float *>(a.fac[a.others[D - 1]]), c.iq);
+    if (D == 3) in.e1.load(reinterpret_cast<const float *>(a.fac[a.others[0]]), c.ie);
   };
   TileIn cur;
   TileCrd crd;  // coordinates of the tile after `cur`
@@ -196,7 +235,7 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
     const uint64_t gi = valid ? t0 + tid : t0;
     const uint32_t row = cur.row;
     const float x = cur.x;
-    const float *p = cur.p, *q = cur.q;
+    const float *p = cur.p.v, *q = cur.q.v;
     // A row `tid`: the Kronecker product p (x) q, rounded to the MMA input type
 #pragma unroll
     for (int c = 0; c < S::KP / S::EPC; ++c) {
@@ -248,6 +287,7 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
 #pragma unroll
     for (int j = 0; j < J; ++j) delta[j] = 0.f;
     {
+      const float *e1 = cur.e1.v;
       float v[S::NP / 16][16];  // the whole lane of the accumulator: all loads, then one wait
 #pragma unroll
       for (int c = 0; c < S::NP / 16; ++c)
@@ -264,7 +304,7 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
           for (int i = 0; i < 16; i += 2) {
             const int col = c * 16 + i;
             if (col < S::ND)
-              acc[col / J] = __ffma2_rn(make_float2(cur.e1[col % J], cur.e1[col % J + 1]),
+              acc[col / J] = __ffma2_rn(make_float2(e1[col % J], e1[col % J + 1]),
                                         make_float2(v[c][i], v[c][i + 1]), acc[col / J]);
           }
         }
@@ -280,7 +320,7 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
               if (D == 2)
                 delta[col] = v[c][i];
               else
-                delta[col / J] += cur.e1[col % J] * v[c][i];
+                delta[col / J] += e1[col % J] * v[c][i];
             }
           }
         }
@@ -289,7 +329,7 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
     tc_fence_before();
     if (KIND == 0) {
       if constexpr (S::GRAM_MMA) {
-        GramMma<J>::store_row(ts.dx + lane * S::LDD, delta, x);
+        GramMma<J>::store_row(ts.dx, lane, delta, x);
       } else {
 #pragma unroll
         for (int j = 0; j < J; ++j) ts.dx[lane * S::LDD + j] = delta[j];
@@ -302,7 +342,7 @@ __device__ __forceinline__ void mode_tc_body(const ModeArgs &a, uint32_t cta, ui
       const int nw = max(0, min(32, nv - warp * 32));  // this warp's valid nonzeros
       if (a.dstore) {  // the warp's delta rows, contiguous in view order
         float *dst = reinterpret_cast<float *>(a.dstore) + (t0 + warp * 32) * J;
-        for (int k = lane; k < nw * J; k += 32) dst[k] = ts.dx[(k / J) * S::LDD + (k % J)];
+        for (int k = lane; k < nw * J; k += 32) dst[k] = ts.dx[tile_off<S>(k / J, k % J)];
       }
       if constexpr (S::GRAM_MMA)
         gram.run(ts.dx, ts.rows + warp * 32, nw, a.gram, S::E, lane);
@@ -443,6 +483,48 @@ int tc_prepare_uncached(const TcLaunch &L, int num_sms, int *grid_cap, int *smem
 
 }  // namespace
 
+// The factor rows the tensor-core kernels gather for `mode` (FRow): the other
+// modes' factors, or for ldf = 12 their gather copies, refreshed here (one launch
+// on the handle's stream) from the factors as they stand.  FRow's 256-bit loads
+// need both on 32-byte boundaries (device allocations are 256-byte aligned;
+// checked, not assumed).
+static int gather_sources(DevTensor &t, int mode, cudaStream_t s, bool refresh, const void *(&src)[kMaxOrder]) {
+  const bool copy = t.ldf == 12;
+  PadList L;
+  memset(&L, 0, sizeof(L));
+  L.first[0] = 0;
+  for (int k = 0; k < t.N; ++k) {
+    src[k] = t.fac[k];
+    if (k == mode) continue;
+    if (copy) {
+      if (!t.gfac[k]) return fail(GTK_ERR_STATE, "tensor-core form without the factors' gather copies");
+      src[k] = t.gfac[k];
+      L.it[L.n] = {reinterpret_cast<const float *>(t.fac[k]), reinterpret_cast<float *>(t.gfac[k])};
+      L.first[L.n + 1] = L.first[L.n] + t.rows[k];
+      ++L.n;
+    }
+    if (reinterpret_cast<uintptr_t>(src[k]) % 32) return fail(GTK_ERR_STATE, "factor rows not on 32-byte boundaries");
+  }
+  if (refresh && L.n && L.first[L.n]) {
+    const uint64_t blocks = std::min<uint64_t>((L.first[L.n] + 255) / 256, 4ull * t.num_sms);
+    k_pad_rows<<<(unsigned)blocks, 256, 0, s>>>(L);
+    GTK_CUDA(cudaGetLastError());
+    t.launches += 1;
+  }
+  return 0;
+}
+
+int tc_gather_items(const DevTensor &t, int mode, std::vector<PadItem> *items, std::vector<uint64_t> *first) {
+  if (t.ldf != 12) return 0;
+  for (int k = 0; k < t.N; ++k) {
+    if (k == mode) continue;
+    if (!t.gfac[k]) return fail(GTK_ERR_STATE, "tensor-core form without the factors' gather copies");
+    items->push_back({reinterpret_cast<const float *>(t.fac[k]), reinterpret_cast<float *>(t.gfac[k])});
+    first->push_back(first->back() + t.rows[k]);
+  }
+  return 0;
+}
+
 // a handle's mode update as one entry of its class's multi-tensor launch (batches)
 int tc_multi_desc(DevTensor &t, int mode, MultiDesc *d) {
   TcLaunch L;
@@ -451,6 +533,8 @@ int tc_multi_desc(DevTensor &t, int mode, MultiDesc *d) {
     return GTK_ERR_UNSUPPORTED;
   }
   if (t.dtype != GTK_F32 || !L.fn_multi) return GTK_ERR_UNSUPPORTED;
+  const void *src[kMaxOrder];
+  if (int rc = gather_sources(t, mode, nullptr, false, src)) return rc;  // the batch refreshes the copies per level
   TcLaunch M = L;
   M.fn = L.fn_multi;  // attributes and residency of the multi-tensor kernel itself
   int cap = 0, smem = 0;
@@ -459,7 +543,7 @@ int tc_multi_desc(DevTensor &t, int mode, MultiDesc *d) {
   memset(&a, 0, sizeof(a));
   for (int k = 0; k < t.N; ++k) {
     a.coord[k] = t.vidx[mode][k];
-    a.fac[k] = t.fac[k];
+    a.fac[k] = src[k];
   }
   a.val = t.vval[mode];
   a.corep = t.corep[mode];
@@ -504,6 +588,8 @@ int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
                               : tc_choose<2>(L, t.precision, t.N, t.J);
   if (!ok && ts_supported(t.N, t.J, t.dtype, t.precision)) return run_mode_tcs(t, mode, kind, out, grid_used);
   if (!ok || t.dtype != GTK_F32) return fail(GTK_ERR_UNSUPPORTED, "no tensor-core form for this shape");
+  const void *src[kMaxOrder];
+  if (int rc = gather_sources(t, mode, t.stream, true, src)) return rc;
   int cap = 0, smem = 0;
   if (int rc = tc_prepare(L, t.num_sms, &cap, &smem)) return rc;
   ModeArgs a;
@@ -511,7 +597,7 @@ int run_mode_tc(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   const ViewRange vr = view_of(t, mode);
   for (int k = 0; k < t.N; ++k) {
     a.coord[k] = vr.coord[k];
-    a.fac[k] = t.fac[k];
+    a.fac[k] = src[k];
   }
   a.val = vr.val;
   a.corep = t.corep[mode];
