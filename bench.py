@@ -457,6 +457,7 @@ def run_batch(args, dist):
         t0 = time.perf_counter()
         variants = [t.autotune() for t in ts]
         tune_s = time.perf_counter() - t0
+        shapes = [t.ctas_per_sm() for t in ts]  # the tile shapes the autotuner kept
         for t in ts:
             t.init_random(1, 0)
         with gtk.Batch(ts) as b:
@@ -504,6 +505,7 @@ def run_batch(args, dist):
             t.set_graph(False)
         res[form] = dict(wall=dist.max(wall), fits=fits, clocks=clk, kernels=kernels, solo=dist.max(solo), tc=tc,
                          tune_s=tune_s, variants={v: variants.count(v) for v in set(variants)},
+                         shapes={str(c): shapes.count(c) for c in set(shapes)},
                          branches=branches, branch_kernels=branch_kernels)
     fast = forms[-1]
     # the plain FP32 form's own run-to-run spread (order of FP64 atomic adds): on
@@ -583,6 +585,7 @@ def run_batch(args, dist):
                           None if v["solo"] is None else v["solo"] / (v["wall"] / args.steps),
                           "graph_kernels": v["kernels"],
                           "tensors_on_tensor_cores": v["tc"], "autotune_s": v["tune_s"], "variants": v["variants"],
+                          "tile_shapes_ctas_per_sm": v.get("shapes"),
                           "ms_per_sweep_repeats": v.get("walls"),
                           "fused_ms_per_sweep": None if v.get("branches") is None else 1e3 * v["branches"],
                           "fused_kernels": v.get("branch_kernels")}

@@ -138,6 +138,8 @@ SIGNATURES = {
     "gtk_set_kernel_variant": (C.c_int, [P, C.c_int]),
     "gtk_get_kernel_variant": (C.c_int, [P, C.POINTER(C.c_int)]),
     "gtk_autotune": (C.c_int, [P, C.POINTER(C.c_int)]),
+    "gtk_set_ctas_per_sm": (C.c_int, [P, C.c_int]),
+    "gtk_get_ctas_per_sm": (C.c_int, [P, C.POINTER(C.c_int)]),
     "gtk_batch_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),
     "gtk_batch_sweep": (C.c_int, [P, C.POINTER(C.c_double)]),
     "gtk_batch_kernels": (C.c_int, [P, U64P]),

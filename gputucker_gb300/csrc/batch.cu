@@ -43,7 +43,7 @@ struct gtk_batch {
   int dev = 0;
   int count = 0;
   std::vector<gtk_tensor *> ts;
-  std::vector<std::pair<int, int>> captured;  // (precision, variant) of each tensor in the graph
+  std::vector<std::tuple<int, int, int>> captured;  // (precision, variant, CTAs per SM) of each tensor in the graph
   cudaStream_t stream = nullptr;
   cudaEvent_t fork = nullptr;
   std::vector<cudaEvent_t> joins;
@@ -76,10 +76,11 @@ __global__ void k_batch_gather(const double *const *__restrict__ errp, int *cons
 
 using TuneKey = std::tuple<int, int, int, int, int, int>;
 std::mutex g_tune_mutex;
-std::map<TuneKey, int> g_tune_cache;
+std::map<TuneKey, std::pair<int, int>> g_tune_cache;  // (variant, CTAs per SM)
 
-int time_update(gtk_tensor *t, int variant, void *save, size_t bytes, double *ms) {
+int time_update(gtk_tensor *t, int variant, int ctas, void *save, size_t bytes, double *ms) {
   t->variant = variant;
+  t->ctas_per_sm = ctas;
   // warm (the first launch of a kernel sets its attributes), then time two updates of mode 0
   if (int rc = run_update_mode(*t, 0)) return rc;
   GTK_CUDA(cudaMemcpyAsync(t->fac[0], save, bytes, cudaMemcpyDeviceToDevice, t->stream));
@@ -177,7 +178,7 @@ int capture(gtk_batch *b) {
   }
   b->graph_kernels = kernels;
   b->captured.clear();
-  for (gtk_tensor *t : b->ts) b->captured.emplace_back(t->precision, t->variant);
+  for (gtk_tensor *t : b->ts) b->captured.emplace_back(t->precision, t->variant, t->ctas_per_sm);
   return 0;
 }
 
@@ -206,6 +207,20 @@ int gtk_get_kernel_variant(const gtk_tensor *t, int *variant) {
   return 0;
 }
 
+int gtk_set_ctas_per_sm(gtk_tensor *t, int ctas) {
+  if (!t) return fail(GTK_ERR_ARG, "null tensor");
+  if (ctas < 0) return fail(GTK_ERR_ARG, "CTAs per SM must be >= 0");
+  t->ctas_per_sm = ctas;
+  drop_graph(*t);
+  return 0;
+}
+
+int gtk_get_ctas_per_sm(const gtk_tensor *t, int *ctas) {
+  if (!t || !ctas) return fail(GTK_ERR_ARG, "null argument");
+  *ctas = t->ctas_per_sm;
+  return 0;
+}
+
 int gtk_autotune(gtk_tensor *t, int *variant) {
   if (!t) return fail(GTK_ERR_ARG, "null tensor");
   if (!t->have_factors || !t->have_core) return fail(GTK_ERR_STATE, "factors and core are not initialised");
@@ -217,13 +232,14 @@ int gtk_autotune(gtk_tensor *t, int *variant) {
     const int b_mean = (int)std::floor(std::log2(std::max(1.0, mean)));
     const int b_skew = (int)std::floor(std::log2(std::max(1.0, maxc / std::max(1.0, mean))));
     const TuneKey key{t->N, t->J, t->dtype, t->precision, b_mean, b_skew};
-    int best = kVarAuto;
+    int best = kVarAuto, best_ctas = 0;
     bool cached = false;
     {
       std::lock_guard<std::mutex> lock(g_tune_mutex);
       auto it = g_tune_cache.find(key);
       if (it != g_tune_cache.end()) {
-        best = it->second;
+        best = it->second.first;
+        best_ctas = it->second.second;
         cached = true;
       }
     }
@@ -238,22 +254,29 @@ int gtk_autotune(gtk_tensor *t, int *variant) {
       int rc = ck(cudaMemcpyAsync(save, t->fac[0], bytes, cudaMemcpyDeviceToDevice, t->stream), "save");
       const bool prof = t->prof;
       t->prof = false;
+      // tile shape: the grid at as many CTAs per SM as fit (0), and at 2 and 1 --
+      // fewer, longer-lived CTAs (more tiles each, fewer contending for an SM's
+      // shared memory, L1 and tensor pipe); values at or above what fits equal 0
+      const int ctas_cands[] = {0, 2, 1};
       double best_ms = 1e300;
-      for (int v : cands) {
-        if (rc) break;
-        double ms = 0;
-        rc = time_update(t, v, save, bytes, &ms);
-        if (!rc && ms < best_ms) {
-          best_ms = ms;
-          best = v;
+      for (int v : cands)
+        for (int c : ctas_cands) {
+          if (rc) break;
+          double ms = 0;
+          rc = time_update(t, v, c, save, bytes, &ms);
+          if (!rc && ms < best_ms * 0.97) {  // a shape other than the first must win by 3 %
+            best_ms = ms;
+            best = v;
+            best_ctas = c;
+          }
         }
-      }
       t->prof = prof;
       const int rc2 = ck(cudaMemcpyAsync(t->fac[0], save, bytes, cudaMemcpyDeviceToDevice, t->stream), "restore");
       const int rc3 = ck(cudaStreamSynchronize(t->stream), "cudaStreamSynchronize");
       cudaFree(save);
       if (rc || rc2 || rc3) {
         t->variant = kVarAuto;
+        t->ctas_per_sm = 0;
         drop_graph(*t);
         return rc ? rc : rc2 ? rc2 : rc3;
       }
@@ -261,9 +284,10 @@ int gtk_autotune(gtk_tensor *t, int *variant) {
       // behalf; the status word belongs to the caller's next real update
       GTK_CUDA(cudaMemset(t->status, 0, 4));
       std::lock_guard<std::mutex> lock(g_tune_mutex);
-      g_tune_cache[key] = best;
+      g_tune_cache[key] = {best, best_ctas};
     }
     t->variant = best;
+    t->ctas_per_sm = best_ctas;
     fit_invalidate(*t);
     drop_graph(*t);
     if (variant) *variant = best;
@@ -321,7 +345,8 @@ int gtk_batch_sweep(gtk_batch *b, double *fits) {
   try {
     if (b->gexec) {
       for (int i = 0; i < b->count && b->gexec; ++i)
-        if (b->captured[i] != std::make_pair(b->ts[i]->precision, b->ts[i]->variant)) drop_batch_graph(b);
+        if (b->captured[i] != std::make_tuple(b->ts[i]->precision, b->ts[i]->variant, b->ts[i]->ctas_per_sm))
+          drop_batch_graph(b);
     }
     if (b->fused) {
       for (int i = 0; i < b->count && b->fused; ++i)

@@ -202,6 +202,7 @@ struct DevTensor {
   unsigned int *nfallback = nullptr;
   uint64_t launches = 0;        // kernels launched by the sweep entry points
   int variant = -1;             // update kernel: kVarAuto or one the autotuner picked
+  int ctas_per_sm = 0;          // update kernels' grids: CTAs per SM (0: as many as fit)
   bool use_graph = false;       // gtk_sweep replays a captured CUDA graph
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t gexec = nullptr;
@@ -280,6 +281,13 @@ struct DevBuf {
 
 // ---- batches: kernels shared by many handles per launch (gtk_batch_sweep)
 constexpr size_t kModeArgsBytes = 320;
+// the grid cap of an update kernel that fits per_sm CTAs on an SM: the handle's
+// CTAs per SM (gtk_set_ctas_per_sm, the autotuner's tile-shape choice) where set
+inline uint64_t update_grid_cap(const DevTensor &t, uint64_t per_sm) {
+  if (t.ctas_per_sm > 0 && (uint64_t)t.ctas_per_sm < per_sm) per_sm = (uint64_t)t.ctas_per_sm;
+  return per_sm * (uint64_t)t.num_sms;
+}
+
 // Gather copies of FP32 factor rows of 12 floats (48 bytes, every other one off
 // a 32-byte boundary) as 64-byte rows, which the tensor-core kernels read with
 // one 256-bit load and one 64- or 128-bit load: two sector accesses per row

@@ -1154,7 +1154,8 @@ template <class V, int KIND> static int launch_mode(DevTensor &t, int mode, void
   GTK_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, L.fn, kThreads, L.smem));
   if (per_sm < 1) return fail(GTK_ERR_UNSUPPORTED, "mode kernel does not fit on an SM");
   const uint64_t ntiles = (a.nnz + L.tn - 1) / L.tn;
-  uint64_t grid = std::min<uint64_t>(ntiles, (uint64_t)per_sm * t.num_sms);
+  uint64_t grid = std::min<uint64_t>(ntiles, KIND == kUpdate ? update_grid_cap(t, (uint64_t)per_sm)
+                                                             : (uint64_t)per_sm * t.num_sms);
   if (KIND == kFit) grid = std::min<uint64_t>(grid, kFitGridMax);
   if (grid < 1) grid = 1;
   void *args[] = {&a};
@@ -1841,7 +1842,7 @@ template <class V> static int spec_multi_desc(DevTensor &t, int mode, MultiDesc 
   d->fn = L.fn_multi;
   d->threads = kThreads;
   d->smem = L.smem;
-  d->ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)per_sm * t.num_sms));
+  d->ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, update_grid_cap(t, (uint64_t)per_sm)));
   d->with_image = false;
   d->image = nullptr;
   memcpy(d->args, &a, sizeof(a));

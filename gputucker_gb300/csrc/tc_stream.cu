@@ -488,7 +488,7 @@ int ts_multi_desc(DevTensor &t, int mode, MultiDesc *d) {
   d->fn = L.fn_multi;
   d->threads = kTsThreads;
   d->smem = (size_t)smem;
-  d->ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, (uint64_t)cap));
+  d->ctas = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(ntiles, update_grid_cap(t, (uint64_t)cap / t.num_sms)));
   d->with_image = true;
   d->image = t.bimg[mode];
   d->tmem = true;
@@ -553,7 +553,7 @@ int run_mode_tcs(DevTensor &t, int mode, int kind, void *out, int *grid_used) {
   for (int k = 0; k < t.N; ++k)
     if (k != mode) a.others[m++] = k;
   const uint64_t ntiles = (a.nnz + kTsThreads - 1) / kTsThreads;
-  uint64_t grid = std::min<uint64_t>(ntiles, (uint64_t)cap);
+  uint64_t grid = std::min<uint64_t>(ntiles, kind == 0 ? update_grid_cap(t, (uint64_t)cap / t.num_sms) : (uint64_t)cap);
   if (kind == 1) grid = std::min<uint64_t>(grid, kTsFitGrid);
   if (grid < 1) grid = 1;
   const unsigned char *img = t.bimg[mode];

@@ -302,10 +302,21 @@ class BlockedTensor:
         return {c: n for n, c in self.VARIANTS.items()}[v.value]
 
     def autotune(self) -> str:
-        """Time the applicable update kernels on mode 0 and keep the fastest (factors unchanged)."""
+        """Time the applicable update kernels on mode 0, each at the tile shapes of
+        ctas_per_sm() in (as many as fit, 2, 1), and keep the fastest pair
+        (factors unchanged); returns the variant."""
         v = C.c_int()
         call("gtk_autotune", self.handle, C.byref(v))
         return {c: n for n, c in self.VARIANTS.items()}[v.value]
+
+    def set_ctas_per_sm(self, ctas: int) -> None:
+        """Size the update kernels' grids for `ctas` CTAs per SM (0: as many as fit)."""
+        call("gtk_set_ctas_per_sm", self.handle, ctas)
+
+    def ctas_per_sm(self) -> int:
+        c = C.c_int()
+        call("gtk_get_ctas_per_sm", self.handle, C.byref(c))
+        return c.value
 
     def tucker_decomposition(self, max_iters: int = 3, tol: float = 1e-4) -> list:
         fits = (C.c_double * max_iters)()

@@ -265,10 +265,14 @@ int gtk_checkpoint_info(const char *path, int *order, int *rank, int *dtype, uin
  * rounded -- FP32 delta bit-identical to the reference's; slow, for parity;
  * selecting it first sums the reference's serial value_t norm on the host).
  * GTK_VARIANT_AUTO: tensor cores for the precision forms, SIMT2 otherwise.  gtk_set_kernel_variant forces one; gtk_autotune times the variants
- * that apply on the handle's mode-0 update (factor 0 restored afterwards), keeps
- * the fastest and caches it per (order, rank, value type, precision, log2 mean
- * row length, log2 longest/mean row length) for the process, so later handles
- * of the same class skip the timing. */
+ * that apply on the handle's mode-0 update (factor 0 restored afterwards), each
+ * at three tile shapes -- grids of as many CTAs per SM as fit, of 2 and of 1
+ * (fewer CTAs, each sweeping more tiles of 128 / 256 / 512 nonzeros) -- keeps
+ * the fastest pair (another than the first must win by 3 %) and caches it per
+ * (order, rank, value type, precision, log2 mean row length, log2 longest/mean
+ * row length) for the process, so later handles of the same class skip the
+ * timing.  gtk_set_ctas_per_sm sets the tile shape directly (0: as many CTAs
+ * per SM as fit, the default; a value above that means the same). */
 #define GTK_VARIANT_AUTO (-1)
 #define GTK_VARIANT_SIMT2 0
 #define GTK_VARIANT_SIMT1 1
@@ -278,6 +282,8 @@ int gtk_checkpoint_info(const char *path, int *order, int *rank, int *dtype, uin
 int gtk_set_kernel_variant(gtk_tensor *t, int variant);
 int gtk_get_kernel_variant(const gtk_tensor *t, int *variant);
 int gtk_autotune(gtk_tensor *t, int *variant);
+int gtk_set_ctas_per_sm(gtk_tensor *t, int ctas);
+int gtk_get_ctas_per_sm(const gtk_tensor *t, int *ctas);
 /* A batch of handles on one device swept together: gtk_batch_sweep runs one
  * sweep (gtk_sweep) of every handle -- the first eagerly, later ones as one
  * replayed CUDA graph whose per-handle branches run concurrently -- and writes

@@ -187,6 +187,46 @@ def test_autotune_keeps_factors_and_caches(ci):
         u.close()
 
 
+@pytest.mark.parametrize("prec", ["plain", "bf16"])
+def test_tile_shape_ctas_per_sm(prec):
+    """The tile-shape axis: one CTA per SM (each CTA sweeps ~20 tiles of the
+    3,125 here) gives the default grid's results up to the order of the Gram
+    rows' FP64 atomic adds; a batch re-captures its graph when a member's shape
+    changes; the autotuner's choice is one of the shapes it times."""
+    case = ([200, 150, 180, 120], [2, 1, 2, 1], 10, 400000, np.float32, prec)
+    ftol, rtol = _tol(np.float32)
+    if prec == "bf16":  # FP32 row solves of weakly determined rank-10 factors (uniform data)
+        rtol = 1e-3
+    t, u = _make(case, 77)
+    try:
+        assert t.ctas_per_sm() == 0
+        with pytest.raises(nat.GTKError):
+            t.set_ctas_per_sm(-1)
+        t.set_ctas_per_sm(1)
+        assert t.ctas_per_sm() == 1
+        ft, fu = t.sweep(), u.sweep()
+        assert abs(ft - fu) <= ftol, (ft, fu)
+        for n in range(4):
+            assert rel_fro(t.get_factor(n), u.get_factor(n)) <= rtol, n
+        ft, fu = t.sweep(), u.sweep()
+        assert abs(ft - fu) <= ftol, (ft, fu)
+        t.set_ctas_per_sm(0)
+        u.init_random(1, 0)
+        with gtk.Batch([t]) as b:
+            t.init_random(1, 0)
+            f0 = [b.sweep()[0] for _ in range(3)]
+            t.set_ctas_per_sm(2)  # the next batch sweep captures a new graph
+            t.init_random(1, 0)
+            f2 = [b.sweep()[0] for _ in range(3)]
+        fu = [u.sweep() for _ in range(3)]
+        assert np.allclose(f0, fu, rtol=0, atol=ftol) and np.allclose(f2, fu, rtol=0, atol=ftol), (f0, f2, fu)
+        u.autotune()
+        assert u.ctas_per_sm() in (0, 1, 2)
+    finally:
+        t.close()
+        u.close()
+
+
 @pytest.mark.parametrize("N,J", [(4, 16), (5, 12), (5, 16)])
 def test_streamed_core_kernels(N, J):
     """Cores too large for shared memory (J^(N-1) * J values) stream through it in
