@@ -138,6 +138,7 @@ SIGNATURES = {
     "gtk_set_kernel_variant": (C.c_int, [P, C.c_int]),
     "gtk_get_kernel_variant": (C.c_int, [P, C.POINTER(C.c_int)]),
     "gtk_autotune": (C.c_int, [P, C.POINTER(C.c_int)]),
+    "gtk_random_sequence": (C.c_int, [C.c_uint32, C.c_uint64, C.c_uint64, C.c_void_p]),
     "gtk_set_ctas_per_sm": (C.c_int, [P, C.c_int]),
     "gtk_get_ctas_per_sm": (C.c_int, [P, C.POINTER(C.c_int)]),
     "gtk_batch_create": (C.c_int, [C.POINTER(P), C.c_int, C.POINTER(P)]),

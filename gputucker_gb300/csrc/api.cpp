@@ -649,27 +649,11 @@ int gtk_init_random(gtk_tensor *t, uint32_t seed, uint64_t skip) {
   if (int rc = set_dev(t)) return rc;
   GTK_GUARD_BEGIN
   GlibcRand g(seed);
-  for (uint64_t k = 0; k < skip; ++k) g.next();
-  const int J = t->J;
-  // tucker.cuh:84-97: mode, slab, real rows of the slab, column
-  for (int n = 0; n < t->N; ++n) {
-    std::vector<unsigned char> slab(t->rows[n] * J * t->vsize, 0);
-    for (uint32_t p = 0; p < t->P[n]; ++p) {
-      uint32_t rows = t->bd[n];
-      if (p + 1 == t->P[n]) rows = t->dims[n] - p * t->bd[n];
-      for (uint32_t r = 0; r < rows; ++r)
-        for (int c = 0; c < J; ++c) {
-          const double v = g.frand01<double>();
-          const uint64_t off = ((uint64_t)p * t->bd[n] + r) * J + c;
-          if (t->dtype == GTK_F32)
-            ((float *)slab.data())[off] = (float)v;
-          else
-            ((double *)slab.data())[off] = v;
-        }
-    }
-    if (int rc = put_factor(*t, n, slab.data())) return rc;
-  }
-  // tucker.cuh:117-134: core in linear order
+  g.jump(skip);
+  // tucker.cuh:84-97 (the factors, generated on the device), then
+  // tucker.cuh:117-134: the core in linear order
+  fit_invalidate(*t);
+  if (int rc = factor_init_device(*t, g)) return rc;
   std::vector<unsigned char> core(t->core_n * t->vsize);
   for (uint64_t i = 0; i < t->core_n; ++i) {
     const double v = g.frand01<double>();
@@ -680,6 +664,31 @@ int gtk_init_random(gtk_tensor *t, uint32_t seed, uint64_t skip) {
   }
   if (int rc = put_core(*t, core.data())) return rc;
   t->have_factors = true;
+  return 0;
+  GTK_GUARD_END
+}
+
+int gtk_random_sequence(uint32_t rand_seed, uint64_t skip_draws, uint64_t n, double *out) {
+  if (n && !out) return fail(GTK_ERR_ARG, "null output");
+  GTK_GUARD_BEGIN
+  GlibcRand g(rand_seed);
+  g.jump(skip_draws);
+  // by the chunks gtk_init_random's device generation uses: each chunk's draws
+  // from its start state, by the recurrence alone
+  const uint64_t len = 65536;
+  const int chunks = (int)std::max<uint64_t>(1, (n + len - 1) / len);
+  std::vector<uint32_t> st((size_t)chunks * 31);
+  glibc_chunk_states(g, len, chunks, st.data());
+  for (int c = 0; c < chunks; ++c) {
+    uint32_t w[31];
+    for (int j = 0; j < 31; ++j) w[j] = st[31 * (size_t)c + j];
+    const uint64_t b = (uint64_t)c * len, e = std::min<uint64_t>(n, b + len);
+    for (uint64_t d = b; d < e; ++d) {  // r[d] = r[d - 31] + r[d - 3]
+      const int k = (int)((d - b) % 31);
+      w[k] += w[(k + 28) % 31];
+      out[d] = (double)(int)(w[k] >> 1) / 2147483647;
+    }
+  }
   return 0;
   GTK_GUARD_END
 }

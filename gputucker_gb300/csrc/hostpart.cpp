@@ -20,13 +20,96 @@
 #include "internal.h"
 
 namespace gtk {
-namespace {
 
 unsigned host_threads(uint64_t work) {
   unsigned nt = std::thread::hardware_concurrency();
   nt = std::max(1u, std::min<unsigned>(nt, 64));
   return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(nt, work / (1 << 16) + 1));
 }
+
+// glibc's random() (TYPE_3, the generator behind the reference's rand()) is the
+// linear recurrence r[n] = r[n-3] + r[n-31] mod 2^32 from its 34th value on, with
+// characteristic polynomial p(x) = x^31 - x^28 - 1.  For any such sequence
+// r[m + k] = sum_j a_j r[m + j] where x^k mod p(x) = sum_j a_j x^j (p is monic,
+// so the reduction is exact over the integers mod 2^32).  The 31 values after a
+// jump of k are therefore dot products of x^(k+j) mod p, j = 0..30, with the
+// current 31-value window: bit-exact, O(31^2 log k) work.
+namespace {
+struct Poly31 {
+  uint32_t c[31];
+};
+Poly31 poly_mul(const Poly31 &a, const Poly31 &b) {
+  uint32_t t[61] = {};
+  for (int i = 0; i < 31; ++i)
+    for (int j = 0; j < 31; ++j) t[i + j] += a.c[i] * b.c[j];
+  for (int d = 60; d >= 31; --d) {  // x^d = x^(d-3) + x^(d-31) mod p
+    t[d - 3] += t[d];
+    t[d - 31] += t[d];
+  }
+  Poly31 r;
+  for (int i = 0; i < 31; ++i) r.c[i] = t[i];
+  return r;
+}
+Poly31 poly_shift(const Poly31 &a) {  // x * a mod p
+  Poly31 r;
+  const uint32_t top = a.c[30];
+  r.c[0] = top;  // x^31 = x^28 + 1
+  for (int i = 1; i < 31; ++i) r.c[i] = a.c[i - 1];
+  r.c[28] += top;
+  return r;
+}
+Poly31 poly_xpow(uint64_t k) {
+  Poly31 r = {}, b = {};
+  r.c[0] = 1;
+  b.c[1] = 1;
+  for (; k; k >>= 1) {
+    if (k & 1) r = poly_mul(r, b);
+    b = poly_mul(b, b);
+  }
+  return r;
+}
+}  // namespace
+
+void GlibcRand::jump(uint64_t k) {
+  if (k < 512) {
+    for (uint64_t s = 0; s < k; ++s) step();
+    return;
+  }
+  uint32_t w[31];  // r[i - 31 + j]
+  for (int j = 0; j < 31; ++j) w[j] = ring[(i + j) % 31];
+  Poly31 a = poly_xpow(k);
+  uint32_t nw[31];
+  for (int j = 0; j < 31; ++j) {
+    uint32_t v = 0;
+    for (int m = 0; m < 31; ++m) v += a.c[m] * w[m];
+    nw[j] = v;
+    a = poly_shift(a);
+  }
+  i += k;
+  for (int j = 0; j < 31; ++j) ring[(i + j) % 31] = nw[j];
+}
+
+void glibc_chunk_states(const GlibcRand &g, uint64_t len, int chunks, uint32_t *out) {
+  uint32_t w[31];  // r[s - 31 + j], s the current chunk start
+  for (int j = 0; j < 31; ++j) w[j] = g.ring[(g.i + j) % 31];
+  if (chunks <= 0) return;
+  Poly31 a0 = poly_xpow(len);
+  for (int c = 0; c < chunks; ++c) {
+    for (int j = 0; j < 31; ++j) out[31 * c + j] = w[j];
+    if (c + 1 == chunks) break;
+    Poly31 a = a0;
+    uint32_t nw[31];
+    for (int j = 0; j < 31; ++j) {
+      uint32_t v = 0;
+      for (int m = 0; m < 31; ++m) v += a.c[m] * w[m];
+      nw[j] = v;
+      a = poly_shift(a);
+    }
+    for (int j = 0; j < 31; ++j) w[j] = nw[j];
+  }
+}
+
+namespace {
 
 template <class F> void par(unsigned nt, F f) {
   std::vector<std::thread> th;

@@ -84,6 +84,8 @@ struct GlibcRand {
   inline int next() { return (int)(step() >> 1); }
   // frand<T>(0, 1) of the reference (helper.hpp:99)
   template <class T> inline T frand01() { return (T(1) - T(0)) * (static_cast<T>(next()) / 2147483647) + T(0); }
+  // advance by k draws without producing them (hostpart.cpp)
+  void jump(uint64_t k);
 };
 
 }  // namespace gtk
@@ -299,6 +301,15 @@ struct PadItem {
 // the copies the tensor-core kernels of `mode` read (none unless ldf = 12),
 // appended with the prefix of their row counts (tc_sweep.cu)
 int tc_gather_items(const DevTensor &t, int mode, std::vector<PadItem> *items, std::vector<uint64_t> *first);
+
+// The 31-value windows r[s - 31 .. s - 1] at the chunk starts s = c * len,
+// c = 0 .. chunks-1, of the stream continuing from g (hostpart.cpp): chunk c's
+// draws follow from out[31 c ..] by the recurrence alone
+void glibc_chunk_states(const GlibcRand &g, uint64_t len, int chunks, uint32_t *out);
+// the draws gtk_init_random places in the factors (tucker.cuh:84-97), generated on
+// the device from chunk states of g, written into the zeroed factors (sweep.cu);
+// afterwards g stands after the factors' draws
+int factor_init_device(DevTensor &t, GlibcRand &g);
 
 // One handle's mode update in the form its kernel class's multi-tensor kernel takes
 struct MultiDesc {

@@ -477,18 +477,22 @@ __global__ void k_where(const uint32_t *__restrict__ keys, const uint32_t *__res
 
 // histogram of (block, local row) into count[b*(bd+1) + row]; one atomic per
 // distinct counter in a warp (heavy rows of a skewed tensor recur within a warp)
-__global__ void k_count_rows(const uint32_t *__restrict__ sbid, const uint32_t *__restrict__ lrow, uint64_t n,
+// count_nnz of mode m from its view: in view order (global row, then
+// block-major position) the nonzeros of one (block, local row) pair form one
+// contiguous run -- a block spans bd consecutive rows, so the local row is
+// row % bd -- and its count is the run's length.  The run's first element adds
+// -p and its last p + 1 (two atomics per run, on distinct counters; the uint64
+// wrap-around leaves the length), against one atomic per nonzero.
+__global__ void k_count_view(const uint32_t *__restrict__ bid, const uint32_t *__restrict__ row, uint64_t n,
                              uint32_t bd, uint64_t *__restrict__ cnt) {
-  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-  const uint64_t start = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const uint64_t rounds = (n + stride - 1) / stride;  // the same for every thread: whole warps stay converged
-  const int lane = threadIdx.x & 31;
-  for (uint64_t r = 0; r < rounds; ++r) {
-    const uint64_t p = start + r * stride;
-    const bool valid = p < n;
-    const unsigned long long c = valid ? (uint64_t)sbid[p] * (bd + 1) + lrow[p] : ~0ull;
-    const uint32_t peers = __match_any_sync(0xFFFFFFFFu, c);
-    if (valid && (peers & ((1u << lane) - 1u)) == 0) atomicAdd((unsigned long long *)&cnt[c], (unsigned long long)__popc(peers));
+  for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t b = bid[p], r = row[p];
+    const bool head = p == 0 || bid[p - 1] != b || row[p - 1] != r;
+    const bool tail = p + 1 == n || bid[p + 1] != b || row[p + 1] != r;
+    if (!head && !tail) continue;
+    unsigned long long *c = (unsigned long long *)&cnt[(uint64_t)b * (bd + 1) + r % bd];
+    if (head) atomicAdd(c, 0ull - (unsigned long long)p);
+    if (tail) atomicAdd(c, (unsigned long long)p + 1ull);
   }
 }
 
@@ -673,12 +677,12 @@ template <class V> int build_impl(DevTensor &t, const gtk_coo &coo) {
       k_gather_view<V><<<G, T, 0, s>>>(t.vperm[m], n, N, gb, vi, (const V *)t.blk_val, (V *)t.vval[m]);
       k_view_block_keys<<<G, T, 0, s>>>(t.vperm[m], sbid, n, keys, perm);
     }
-    TRY(radix_sort(keys, perm, n, bits_for(t.nblk - 1), sc, s));
-    if (n) k_where<<<G, T, 0, s>>>(keys, perm, n, t.blk_ptr, t.where[m]);
-    // count_nnz
+    // count_nnz, from the view order (keys: block ids in view order)
     const uint64_t cm = t.nblk * (uint64_t)(t.bd[m] + 1);
     TRY(ck(cudaMemsetAsync(t.count[m], 0, cm * 8, s), "memset"));
-    if (n) k_count_rows<<<G, T, 0, s>>>(sbid, t.blk_idx[m], n, t.bd[m], t.count[m]);
+    if (n) k_count_view<<<G, T, 0, s>>>(keys, t.vidx[m][m], n, t.bd[m], t.count[m]);
+    TRY(radix_sort(keys, perm, n, bits_for(t.nblk - 1), sc, s));
+    if (n) k_where<<<G, T, 0, s>>>(keys, perm, n, t.blk_ptr, t.where[m]);
     TRY(exclusive_scan<unsigned long long>((unsigned long long *)t.count[m], cm, (unsigned long long *)sc.sums, s));
     k_count_rebase<<<grid_for(cm, T, t.num_sms), T, 0, s>>>(t.count[m], t.nblk, t.bd[m], t.blk_ptr);
     TRY(ck(cudaGetLastError(), "segmenting"));

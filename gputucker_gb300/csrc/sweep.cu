@@ -1514,6 +1514,103 @@ int factor_to_host(const DevTensor &t, int n, void *slabs) {
   return 0;
 }
 
+// The factors' draws of gtk_init_random (tucker.cuh:84-97): mode n's real rows
+// are rows 0 .. dims[n]-1 of its stacked slabs, so draw d of the mode lands at
+// row d / J, column d % J.  Two passes over the zeroed factors:
+// * k_fac_draws: thread c generates draws [c len, (c+1) len) of the sequence from
+//   its 31-value start window by glibc's recurrence r[k] = r[k-31] + r[k-3]
+//   (mod 2^32), 31 steps at a time so the window stays in registers, and stores
+//   rand() = r >> 1 in the draw's factor entry as an integer;
+// * k_fac_frand: every entry of the factors, in parallel, becomes
+//   frand(0, 1) = (double)rand() / (2^31 - 1) as value_t (padding entries hold 0
+//   and stay 0), so the FP64 divisions spread over the whole GPU.
+struct FacInit {
+  void *fac[kMaxOrder];
+  uint64_t first[kMaxOrder + 1];  // draw offset of each mode
+  int N, J, ldf;
+};
+template <class V>
+__global__ void k_fac_draws(const uint32_t *__restrict__ states, int chunks, uint64_t len, const __grid_constant__ FacInit f) {
+  using U = std::conditional_t<sizeof(V) == 4, uint32_t, unsigned long long>;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= chunks) return;
+  uint32_t w[31];
+#pragma unroll
+  for (int j = 0; j < 31; ++j) w[j] = states[31 * (size_t)c + j];
+  const uint64_t b = (uint64_t)c * len, e = min(f.first[f.N], b + len);
+  int n = 0;
+  while (n + 1 < f.N && b >= f.first[n + 1]) ++n;
+  const uint64_t off = b - f.first[n];
+  uint64_t row = off / (uint64_t)f.J;
+  int col = (int)(off - row * (uint64_t)f.J);
+  for (uint64_t base = b; base < e; base += 31) {
+#pragma unroll
+    for (int k = 0; k < 31; ++k) {
+      const uint32_t v = w[k] + w[(k + 28) % 31];
+      w[k] = v;
+      if (base + k < e) {
+        while (base + k >= f.first[n + 1]) {  // the next mode's draws
+          ++n;
+          row = 0;
+          col = 0;
+        }
+        reinterpret_cast<U *>(f.fac[n])[row * (uint64_t)f.ldf + col] = (U)(v >> 1);
+        if (++col == f.J) {
+          col = 0;
+          ++row;
+        }
+      }
+    }
+  }
+}
+template <class V> __global__ void k_fac_frand(V *__restrict__ fac, uint64_t m) {
+  using U = std::conditional_t<sizeof(V) == 4, uint32_t, unsigned long long>;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < m; i += (uint64_t)gridDim.x * blockDim.x) {
+    const U r = reinterpret_cast<const U *>(fac)[i];
+    fac[i] = (V)((double)r / 2147483647.0);
+  }
+}
+
+int factor_init_device(DevTensor &t, GlibcRand &g) {
+  FacInit f;
+  memset(&f, 0, sizeof(f));
+  f.N = t.N;
+  f.J = t.J;
+  f.ldf = t.ldf;
+  for (int n = 0; n < t.N; ++n) {
+    f.fac[n] = t.fac[n];
+    f.first[n + 1] = f.first[n] + (uint64_t)t.dims[n] * t.J;
+    GTK_CUDA(cudaMemsetAsync(t.fac[n], 0, t.rows[n] * (uint64_t)t.ldf * t.vsize, t.stream));
+  }
+  const uint64_t total = f.first[t.N];
+  if (!total) return 0;
+  const uint64_t len = 16384;
+  const int chunks = (int)((total + len - 1) / len);
+  std::vector<uint32_t> st((size_t)chunks * 31);
+  glibc_chunk_states(g, len, chunks, st.data());
+  DevBuf buf;
+  GTK_CUDA(buf.alloc(st.size() * 4));
+  GTK_CUDA(cudaMemcpyAsync(buf.p, st.data(), st.size() * 4, cudaMemcpyHostToDevice, t.stream));
+  const unsigned blocks = (unsigned)((chunks + 31) / 32);
+  if (t.dtype == GTK_F32)
+    k_fac_draws<float><<<blocks, 32, 0, t.stream>>>(buf.as<uint32_t>(), chunks, len, f);
+  else
+    k_fac_draws<double><<<blocks, 32, 0, t.stream>>>(buf.as<uint32_t>(), chunks, len, f);
+  GTK_CUDA(cudaGetLastError());
+  for (int n = 0; n < t.N; ++n) {
+    const uint64_t m = t.rows[n] * (uint64_t)t.ldf;
+    const unsigned gr = (unsigned)std::min<uint64_t>((m + 255) / 256, (uint64_t)t.num_sms * 8);
+    if (t.dtype == GTK_F32)
+      k_fac_frand<float><<<gr, 256, 0, t.stream>>>((float *)t.fac[n], m);
+    else
+      k_fac_frand<double><<<gr, 256, 0, t.stream>>>((double *)t.fac[n], m);
+    GTK_CUDA(cudaGetLastError());
+  }
+  GTK_CUDA(cudaStreamSynchronize(t.stream));  // the states' buffer is freed on return
+  g.jump(total);
+  return 0;
+}
+
 int factor_from_host(DevTensor &t, int n, const void *slabs) {
   const uint64_t m = t.rows[n] * (uint64_t)t.J;
   if (!m) return 0;

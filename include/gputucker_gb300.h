@@ -150,6 +150,13 @@ void gtk_destroy(gtk_tensor *t);
  * slab, column 0..J-1, then the J^N core entries in linear order.  Padding rows
  * of the last slab are 0. */
 int gtk_init_random(gtk_tensor *t, uint32_t rand_seed, uint64_t skip_draws);
+/* The draws gtk_init_random places, in that order: n values of frand<double>(0,1)
+ * from the glibc rand() stream of `rand_seed` after `skip_draws` draws.
+ * gtk_init_random generates the factors' draws on the device, in chunks whose
+ * start states come from jumps in the generator's linear recurrence
+ * (r[k] = r[k-3] + r[k-31] mod 2^32); this function runs the same chunks on the
+ * host (no device). */
+int gtk_random_sequence(uint32_t rand_seed, uint64_t skip_draws, uint64_t n, double *out);
 /* slab layout [P_n * block_dims[n]][J], element type = dtype */
 int gtk_set_factor(gtk_tensor *t, int mode, const void *slabs);
 int gtk_get_factor(const gtk_tensor *t, int mode, void *slabs);

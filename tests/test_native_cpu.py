@@ -309,3 +309,20 @@ def test_checkpoint_info_rejects_garbage(native, tmp_path):
     assert native.gtk_checkpoint_info(str(p).encode(), None, None, None, None, None, None) == nat.GTK_ERR_PARSE
     assert native.gtk_checkpoint_info(str(tmp_path / "missing").encode(), None, None, None, None, None,
                                       None) == nat.GTK_ERR_IO
+
+
+@pytest.mark.parametrize("seed,skip,n", [(1, 0, 1000), (7, 123, 300_000), (2**31 + 5, 1_000_007, 200_000)])
+def test_random_sequence_jump_ahead(seed, skip, n):
+    """gtk_random_sequence (the draws gtk_init_random places) splits the draws over
+    host threads, each jumping ahead in glibc's additive recurrence; the values
+    must equal frand(0, 1) = rand() / (2^31 - 1) of the C library's own rand()
+    stream, draw for draw, whatever the chunk boundaries."""
+    libc = C.CDLL("libc.so.6")
+    libc.srand.argtypes = [C.c_uint]
+    libc.srand(seed & 0xFFFFFFFF)
+    for _ in range(skip):
+        libc.rand()
+    want = np.array([libc.rand() for _ in range(n)], np.float64) / 2147483647.0
+    got = np.empty(n, np.float64)
+    nat.call("gtk_random_sequence", seed & 0xFFFFFFFF, skip, n, got.ctypes.data)
+    np.testing.assert_array_equal(got, want)
