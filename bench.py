@@ -142,6 +142,55 @@ class Dist:
 
 
 # ------------------------------------------------------------------ clocks
+class _NvmlSampler:
+    """SM clock, maximum SM clock and clock-event reasons read through NVML every
+    10 ms on a host thread (read-only queries), so that even a timed region of a
+    few hundred milliseconds carries tens of samples."""
+    REASONS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+
+    def __init__(self, device: int):
+        import ctypes as C
+        import threading
+        lib = C.CDLL("libnvidia-ml.so.1")
+        if lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit")
+        self.lib, self.C = lib, C
+        self.h = C.c_void_p()
+        if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(device), C.byref(self.h)) != 0:
+            raise RuntimeError("nvmlDeviceGetHandleByIndex")
+        mx = C.c_uint()
+        if lib.nvmlDeviceGetMaxClockInfo(self.h, C.c_int(1), C.byref(mx)) != 0:  # NVML_CLOCK_SM
+            raise RuntimeError("nvmlDeviceGetMaxClockInfo")
+        try:
+            self.reasons_fn = lib.nvmlDeviceGetCurrentClocksEventReasons
+        except AttributeError:
+            self.reasons_fn = lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        self.mx = float(mx.value)
+        self.sm, self.mask = [], 0
+        self.done = threading.Event()
+        self.t = threading.Thread(target=self._run, daemon=True)
+        self.t.start()
+
+    def _run(self):
+        C, lib = self.C, self.lib
+        clk, why = C.c_uint(), C.c_ulonglong()
+        while not self.done.is_set():
+            if lib.nvmlDeviceGetClockInfo(self.h, C.c_int(1), C.byref(clk)) == 0:
+                self.sm.append(float(clk.value))
+            if self.reasons_fn(self.h, C.byref(why)) == 0:
+                self.mask |= why.value
+            self.done.wait(0.01)
+
+    def stop(self):
+        self.done.set()
+        self.t.join()
+        if not self.sm:
+            return None
+        reasons = sorted(n for n, b in self.REASONS.items() if self.mask & b)
+        return {"sm_mhz": statistics.median(self.sm), "sm_max_mhz": self.mx, "reasons": reasons,
+                "samples": len(self.sm), "source": "nvml, 10 ms"}
+
+
 class Clocks:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
@@ -149,6 +198,12 @@ class Clocks:
 
     def __init__(self, device: int):
         self.p = None
+        self.nvml = None
+        try:
+            self.nvml = _NvmlSampler(device)
+            return
+        except Exception:
+            self.nvml = None
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
                                        "-lms", "200", "-i", str(device)], stdout=subprocess.PIPE,
@@ -157,6 +212,8 @@ class Clocks:
             self.p = None
 
     def stop(self):
+        if self.nvml is not None:
+            return self.nvml.stop()
         if self.p is None:
             return None
         self.p.terminate()
