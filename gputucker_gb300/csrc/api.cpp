@@ -673,22 +673,35 @@ int gtk_random_sequence(uint32_t rand_seed, uint64_t skip_draws, uint64_t n, dou
   GTK_GUARD_BEGIN
   GlibcRand g(rand_seed);
   g.jump(skip_draws);
-  // by the chunks gtk_init_random's device generation uses: each chunk's draws
-  // from its start state, by the recurrence alone
-  const uint64_t len = 65536;
-  const int chunks = (int)std::max<uint64_t>(1, (n + len - 1) / len);
-  std::vector<uint32_t> st((size_t)chunks * 31);
-  glibc_chunk_states(g, len, chunks, st.data());
-  for (int c = 0; c < chunks; ++c) {
-    uint32_t w[31];
-    for (int j = 0; j < 31; ++j) w[j] = st[31 * (size_t)c + j];
-    const uint64_t b = (uint64_t)c * len, e = std::min<uint64_t>(n, b + len);
-    for (uint64_t d = b; d < e; ++d) {  // r[d] = r[d - 31] + r[d - 3]
-      const int k = (int)((d - b) % 31);
-      w[k] += w[(k + 28) % 31];
-      out[d] = (double)(int)(w[k] >> 1) / 2147483647;
+  // by the split gtk_init_random's device generation uses: chunk start windows,
+  // each chunk's pieces moved on from them by the step polynomials, each piece's
+  // draws by the recurrence alone
+  const uint64_t len = kFacChunk / kFacSplit;
+  const int chunks = (int)std::max<uint64_t>(1, (n + kFacChunk - 1) / kFacChunk);
+  std::vector<uint32_t> st((size_t)chunks * 31), pol((size_t)kFacSplit * 31);
+  glibc_chunk_states(g, kFacChunk, chunks, st.data());
+  glibc_step_polys(len, kFacSplit, pol.data());
+  for (int c = 0; c < chunks; ++c)
+    for (int piece = 0; piece < kFacSplit; ++piece) {
+      const uint64_t b = (uint64_t)c * kFacChunk + (uint64_t)piece * len, e = std::min<uint64_t>(n, b + len);
+      if (b >= e) break;
+      uint32_t a[31], w[31];
+      for (int j = 0; j < 31; ++j) a[j] = pol[31 * (size_t)piece + j];
+      for (int m = 0; m < 31; ++m) {  // w[m] = (x^(piece len + m) mod p) . chunk window
+        uint32_t v = 0;
+        for (int j = 0; j < 31; ++j) v += a[j] * st[31 * (size_t)c + j];
+        w[m] = v;
+        const uint32_t top = a[30];
+        for (int j = 30; j > 0; --j) a[j] = a[j - 1];
+        a[0] = top;
+        a[28] += top;
+      }
+      for (uint64_t d = b; d < e; ++d) {  // r[d] = r[d - 31] + r[d - 3]
+        const int k = (int)((d - b) % 31);
+        w[k] += w[(k + 28) % 31];
+        out[d] = (double)(int)(w[k] >> 1) / 2147483647;
+      }
     }
-  }
   return 0;
   GTK_GUARD_END
 }

@@ -89,6 +89,16 @@ void GlibcRand::jump(uint64_t k) {
   for (int j = 0; j < 31; ++j) ring[(i + j) % 31] = nw[j];
 }
 
+void glibc_step_polys(uint64_t step, int count, uint32_t *out) {
+  Poly31 a = {};
+  a.c[0] = 1;  // x^0
+  const Poly31 s = poly_xpow(step);
+  for (int j = 0; j < count; ++j) {
+    for (int m = 0; m < 31; ++m) out[31 * j + m] = a.c[m];
+    a = poly_mul(a, s);
+  }
+}
+
 void glibc_chunk_states(const GlibcRand &g, uint64_t len, int chunks, uint32_t *out) {
   uint32_t w[31];  // r[s - 31 + j], s the current chunk start
   for (int j = 0; j < 31; ++j) w[j] = g.ring[(g.i + j) % 31];

@@ -306,6 +306,14 @@ int tc_gather_items(const DevTensor &t, int mode, std::vector<PadItem> *items, s
 // c = 0 .. chunks-1, of the stream continuing from g (hostpart.cpp): chunk c's
 // draws follow from out[31 c ..] by the recurrence alone
 void glibc_chunk_states(const GlibcRand &g, uint64_t len, int chunks, uint32_t *out);
+// coefficients of x^(j step) mod (x^31 - x^28 - 1), j = 0 .. count-1, 31 words
+// each: applied to a chunk's start window they give the window j steps of
+// `step` draws further on (the device splits each chunk by them)
+void glibc_step_polys(uint64_t step, int count, uint32_t *out);
+// the device generation's split: chunks of kFacChunk draws (start windows from
+// the host), each cut into kFacSplit pieces of one thread each
+constexpr uint64_t kFacChunk = 16384;
+constexpr int kFacSplit = 16;
 // the draws gtk_init_random places in the factors (tucker.cuh:84-97), generated on
 // the device from chunk states of g, written into the zeroed factors (sweep.cu);
 // afterwards g stands after the factors' draws

@@ -1517,10 +1517,14 @@ int factor_to_host(const DevTensor &t, int n, void *slabs) {
 // The factors' draws of gtk_init_random (tucker.cuh:84-97): mode n's real rows
 // are rows 0 .. dims[n]-1 of its stacked slabs, so draw d of the mode lands at
 // row d / J, column d % J.  Two passes over the zeroed factors:
-// * k_fac_draws: thread c generates draws [c len, (c+1) len) of the sequence from
-//   its 31-value start window by glibc's recurrence r[k] = r[k-31] + r[k-3]
-//   (mod 2^32), 31 steps at a time so the window stays in registers, and stores
-//   rand() = r >> 1 in the draw's factor entry as an integer;
+// * k_fac_draws: the sequence is cut into chunks of kFacChunk draws (start
+//   windows from the host) and each chunk into kFacSplit pieces; thread
+//   (c, j) moves chunk c's 31-value window on by j pieces (the window of x^k mod
+//   p applied to it: the coefficients of x^(j len) mod p come from the host,
+//   then one multiplication by x per further value), then generates its piece by
+//   glibc's recurrence r[k] = r[k-31] + r[k-3] (mod 2^32), 31 steps at a time so
+//   the window stays in registers, and stores rand() = r >> 1 in the draw's
+//   factor entry as an integer;
 // * k_fac_frand: every entry of the factors, in parallel, becomes
 //   frand(0, 1) = (double)rand() / (2^31 - 1) as value_t (padding entries hold 0
 //   and stay 0), so the FP64 divisions spread over the whole GPU.
@@ -1530,14 +1534,33 @@ struct FacInit {
   int N, J, ldf;
 };
 template <class V>
-__global__ void k_fac_draws(const uint32_t *__restrict__ states, int chunks, uint64_t len, const __grid_constant__ FacInit f) {
+__global__ void k_fac_draws(const uint32_t *__restrict__ states, const uint32_t *__restrict__ polys, int chunks,
+                            const __grid_constant__ FacInit f) {
   using U = std::conditional_t<sizeof(V) == 4, uint32_t, unsigned long long>;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  constexpr uint64_t len = kFacChunk / kFacSplit;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int c = t / kFacSplit, piece = t % kFacSplit;
   if (c >= chunks) return;
+  const uint64_t b = (uint64_t)c * kFacChunk + (uint64_t)piece * len, e = min(f.first[f.N], b + len);
+  if (b >= e) return;
   uint32_t w[31];
+  {
+    uint32_t s[31], a[31];
 #pragma unroll
-  for (int j = 0; j < 31; ++j) w[j] = states[31 * (size_t)c + j];
-  const uint64_t b = (uint64_t)c * len, e = min(f.first[f.N], b + len);
+    for (int j = 0; j < 31; ++j) s[j] = states[31 * (size_t)c + j], a[j] = polys[31 * piece + j];
+#pragma unroll
+    for (int m = 0; m < 31; ++m) {  // w[m] = r[b - 31 + m] = (x^(piece len + m) mod p) . s
+      uint32_t v = 0;
+#pragma unroll
+      for (int j = 0; j < 31; ++j) v += a[j] * s[j];
+      w[m] = v;
+      const uint32_t top = a[30];  // a <- x a mod p, x^31 = x^28 + 1
+#pragma unroll
+      for (int j = 30; j > 0; --j) a[j] = a[j - 1];
+      a[0] = top;
+      a[28] += top;
+    }
+  }
   int n = 0;
   while (n + 1 < f.N && b >= f.first[n + 1]) ++n;
   const uint64_t off = b - f.first[n];
@@ -1584,18 +1607,19 @@ int factor_init_device(DevTensor &t, GlibcRand &g) {
   }
   const uint64_t total = f.first[t.N];
   if (!total) return 0;
-  const uint64_t len = 16384;
-  const int chunks = (int)((total + len - 1) / len);
-  std::vector<uint32_t> st((size_t)chunks * 31);
-  glibc_chunk_states(g, len, chunks, st.data());
+  const int chunks = (int)((total + kFacChunk - 1) / kFacChunk);
+  std::vector<uint32_t> st((size_t)(chunks + kFacSplit) * 31);  // chunk windows, then the piece polynomials
+  glibc_chunk_states(g, kFacChunk, chunks, st.data());
+  glibc_step_polys(kFacChunk / kFacSplit, kFacSplit, st.data() + (size_t)chunks * 31);
   DevBuf buf;
   GTK_CUDA(buf.alloc(st.size() * 4));
   GTK_CUDA(cudaMemcpyAsync(buf.p, st.data(), st.size() * 4, cudaMemcpyHostToDevice, t.stream));
-  const unsigned blocks = (unsigned)((chunks + 31) / 32);
+  const uint32_t *d_st = buf.as<uint32_t>();
+  const unsigned blocks = (unsigned)(((uint64_t)chunks * kFacSplit + 63) / 64);
   if (t.dtype == GTK_F32)
-    k_fac_draws<float><<<blocks, 32, 0, t.stream>>>(buf.as<uint32_t>(), chunks, len, f);
+    k_fac_draws<float><<<blocks, 64, 0, t.stream>>>(d_st, d_st + (size_t)chunks * 31, chunks, f);
   else
-    k_fac_draws<double><<<blocks, 32, 0, t.stream>>>(buf.as<uint32_t>(), chunks, len, f);
+    k_fac_draws<double><<<blocks, 64, 0, t.stream>>>(d_st, d_st + (size_t)chunks * 31, chunks, f);
   GTK_CUDA(cudaGetLastError());
   for (int n = 0; n < t.N; ++n) {
     const uint64_t m = t.rows[n] * (uint64_t)t.ldf;
