@@ -198,6 +198,46 @@ int parse_buffer(const char *buf, size_t len, int N, int dtype, uint32_t seed, g
     uint64_t line = k.first_line;
     std::string vtok;
     while (p < e) {
+      // One pass over the common line: N plain digit indices (>= 1, at most 19
+      // digits), each followed by a space or tab, then a value token that the
+      // exact decimal path reads.  The chunk holds whole lines, so every scan
+      // stops at the line's '\n'.  Any other line goes to the general code below,
+      // which gives the same results (and the errors) for everything.
+      {
+        const char *s = p;
+        uint32_t iv[kMaxOrder];
+        bool ok = true;
+        for (int n = 0; n < N && ok; ++n) {
+          while (*s == ' ' || *s == '\t') ++s;
+          const char *d0 = s;
+          uint64_t v = 0;
+          for (unsigned d; (d = (unsigned)(*s - '0')) <= 9u; ++s) v = v * 10 + d;
+          const size_t len = (size_t)(s - d0);
+          iv[n] = (uint32_t)v;  // strtoull's value narrowed to uint32, as parse_index
+          ok = len > 0 && len <= 19 && iv[n] >= 1 && (*s == ' ' || *s == '\t');
+        }
+        if (ok) {
+          while (*s == ' ' || *s == '\t') ++s;
+          const char *vs = s;
+          while (*s != '\n' && *s != ' ' && *s != '\t') ++s;
+          double d = 0;
+          ok = s > vs && parse_value_fast(vs, s, d);
+          if (ok) {
+            const char *nl = *s == '\n' ? s : (const char *)memchr(s, '\n', (size_t)(e - s));
+            for (int n = 0; n < N; ++n) {
+              out->idx[n][line] = iv[n] - 1;
+              if (iv[n] > k.maxd[n]) k.maxd[n] = iv[n];
+            }
+            if (dtype == GTK_F32)
+              out->vf[line] = (float)d;
+            else
+              out->vd[line] = d;
+            ++line;
+            p = nl + 1;
+            continue;
+          }
+        }
+      }
       const char *nl = (const char *)memchr(p, '\n', (size_t)(e - p));
       if (!nl) break;
       const char *s = p;

@@ -116,6 +116,44 @@ def test_parser_matches_oracle(native, text, dtype):
     np.testing.assert_array_equal(gv, vals)
 
 
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_parser_mixed_line_forms_match_oracle(native, seed):
+    """Lines in the common form (the parser's one-pass path) mixed with every
+    other form it hands to its general path -- blanks before, between and after
+    tokens, extra columns, signed and zero-padded indices, exponents, CRLF,
+    missing values -- give the oracle's indices, values, dims and draws."""
+    rng = np.random.default_rng(seed)
+    lines = []
+    for i in range(3000):
+        a, b, c = (int(x) for x in rng.integers(1, 50, 3))
+        v = f"{rng.random():.9g}"
+        form = int(rng.integers(0, 10))
+        if form < 4:
+            lines.append(f"{a}\t{b}\t{c}\t{v}\n")
+        elif form == 4:
+            lines.append(f"  {a} \t {b}\t{c}   {v}  \n")
+        elif form == 5:
+            lines.append(f"{a}\t{b}\t{c}\t{v}\textra\t9\n")
+        elif form == 6:
+            lines.append(f"+{a}\t00{b}\t{c}\t{v}e0\n")
+        elif form == 7:
+            lines.append(f"{a}\t{b}\t{c}\t{v}\r\n")
+        elif form == 8:
+            lines.append(f"{a}\t{b}\t{c}\n")  # value drawn from rand()
+        else:
+            lines.append(f"{a} {b} {c} -{v}E-2\n")
+    text = "".join(lines).encode()
+    for dtype in (0, 1):
+        rc, idx, vals, dims, draws = ora_parse(text, 3, dtype, seed=seed)
+        assert rc == 0
+        coo = gtk.parse_buffer(text, 3, dtype, rand_seed=seed)
+        gi, gv = coo.arrays()
+        assert coo.dims == dims and coo.rand_draws == draws
+        for n in range(3):
+            np.testing.assert_array_equal(gi[n], idx[n])
+        np.testing.assert_array_equal(gv, vals)
+
+
 @pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p)[:-4] for p in GOLDEN])
 def test_parser_matches_reference_golden(native, path):
     g = np.load(path)
@@ -135,6 +173,7 @@ def test_parser_matches_reference_golden(native, path):
     (b"1\t2\t3\t0.5\n\n", nat.GTK_ERR_PARSE),       # empty line
     (b"1\t2\t3\tabc\n", nat.GTK_ERR_PARSE),         # value that is not a number
     (b"# comment\n1\t2\t3\t0.5\n", nat.GTK_ERR_PARSE),  # the format has no comments
+    (b"1\t4294967296\t3\t0.5\n", nat.GTK_ERR_PARSE),  # narrows to index 0 as a uint32
 ])
 def test_parser_errors(native, text, code):
     with pytest.raises(gtk.GTKError) as e:
