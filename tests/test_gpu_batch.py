@@ -273,6 +273,9 @@ FUSED = [
     ([30, 28, 26, 24], [1, 1, 1, 1], 16, 20000, np.float32, "bf16"),
     ([60, 50, 40], [2, 1, 1], 12, 15000, np.float32, "plain"),
     ([45, 40, 35], [1, 1, 1], 4, 9000, np.float32, "plain"),
+    # rank 10 on the tensor cores: rows of 12 floats, read from the gather copies
+    # that the fused form refreshes in its per-level zeroing kernel
+    ([40, 36, 30, 28], [1, 1, 2, 1], 10, 20000, np.float32, "bf16"),
 ]
 
 
