@@ -365,3 +365,19 @@ def test_random_sequence_jump_ahead(seed, skip, n):
     got = np.empty(n, np.float64)
     nat.call("gtk_random_sequence", seed & 0xFFFFFFFF, skip, n, got.ctypes.data)
     np.testing.assert_array_equal(got, want)
+
+
+@pytest.mark.parametrize("skip", [10**9 + 3, 2**40 + 12345, 10**12 + 7])
+def test_random_sequence_large_jumps_compose(native, skip):
+    """Jumps far beyond what stepping can check: the draws after skip + 5000 are the
+    draws after skip, 5000 on (x^(a+b) = x^a x^b mod the recurrence's polynomial),
+    and differ from the unskipped stream."""
+    a = np.empty(6000, np.float64)
+    b = np.empty(1000, np.float64)
+    nat.call("gtk_random_sequence", 1, skip, 6000, a.ctypes.data)
+    nat.call("gtk_random_sequence", 1, skip + 5000, 1000, b.ctypes.data)
+    np.testing.assert_array_equal(b, a[5000:])
+    c = np.empty(1000, np.float64)
+    nat.call("gtk_random_sequence", 1, 0, 1000, c.ctypes.data)
+    assert not np.array_equal(a[:1000], c)
+    assert np.all((a >= 0) & (a <= 1))
